@@ -1,0 +1,98 @@
+/*
+ * prec_gpu.h -- C ABI of the GB300 large-operand multiply.
+ *
+ * Drop-in boundary for the two size bands of preclib's multiply dispatcher
+ * that this library replaces:
+ *   precn_t mul_ntt(const precn_t&, const precn_t&)   prec.hpp:102,
+ *       src/mul_ntt.cpp:494 (called from src/mul_basic.cpp:264 for >6144 limbs)
+ *   precn_t mul_fft(const precn_t&, const precn_t&)   prec.hpp:94,
+ *       src/mul_fft.cpp:386 (called from src/mul_basic.cpp:203, 268 for 193-6144 limbs)
+ * Those C++ entry points take and return precn_t {asiz, rsiz, a} with
+ * little-endian uint64 limbs (prec.hpp:49-52).  This header flattens them to
+ * plain pointers and sizes; prec_gpu_precn.cpp rebuilds the C++ symbols on
+ * top of it for a build that links the reference's other sources.
+ *
+ * Limbs: value = a[0] + a[1]*2^64 + ...  The product of an and bn limbs is
+ * written as exactly an+bn limbs (high limbs zero-padded); the caller trims.
+ * Every entry point returns 0 on success or one of the PREC_GPU_E_* codes.
+ * Nothing here falls back to a CPU multiply: without a usable CUDA device
+ * every call fails with PREC_GPU_E_NODEV.
+ */
+#ifndef PREC_GPU_H
+#define PREC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PREC_GPU_OK = 0,
+    PREC_GPU_E_ARG = 1,          /* null pointer, zero or inconsistent size */
+    PREC_GPU_E_TOO_LARGE = 2,    /* product beyond the 2^26-point transform */
+    PREC_GPU_E_NOMEM = 3,        /* device allocation failed */
+    PREC_GPU_E_CUDA = 4,         /* other CUDA runtime error */
+    PREC_GPU_E_TIMEOUT = 5,      /* a bounded device-side wait ran out */
+    PREC_GPU_E_FFT_ROUNDING = 6, /* FP64 band: distance to integer > 0.25 */
+    PREC_GPU_E_NODEV = 7,        /* no CUDA device / library not initialised */
+    PREC_GPU_E_INTERNAL = 8      /* internal consistency check failed */
+};
+
+/* Per-product report of the most recent call on the calling thread. */
+typedef struct prec_gpu_stats {
+    int path;                 /* 0 single-CTA NTT, 1 four-step NTT, 2 FP64 FFT */
+    int log2_n;               /* transform length */
+    size_t limbs_a, limbs_b;  /* operand sizes used */
+    double fft_max_distance;  /* FP64 band: max |x - round(x)|; 0 for NTT */
+    double device_ms;         /* device time of the product (events) */
+} prec_gpu_stats_t;
+
+/* Selects and initialises the device (idempotent; device -1 = current).
+ * Replaces: nothing (the reference keeps thread_local NTT plans,
+ * src/mul_ntt.cpp:182-191, and a static FFT plan cache, src/mul_fft.cpp:78-100). */
+int prec_gpu_init(int device);
+
+/* Releases every device resource of the library. */
+void prec_gpu_shutdown(void);
+
+/* Full product of two host limb vectors, out[0 .. an+bn) written.
+ * Band routing inside: max(an,bn) <= 6144 limbs -> FP64 FFT band
+ * (replaces mul_fft, src/mul_fft.cpp:386-394), larger -> NTT band
+ * (replaces mul_ntt, src/mul_ntt.cpp:494-518).  Squares above 6144 limbs
+ * and products of any size below 193 limbs also run on the GPU.
+ * Thread-safe (calls are serialised on one device context). */
+int prec_gpu_mul(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uint64_t *out);
+
+/* NTT band forced, host pointers (replaces mul_ntt, src/mul_ntt.cpp:494). */
+int prec_gpu_mul_ntt(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uint64_t *out);
+
+/* Same product on device pointers, enqueued on `stream` (a cudaStream_t;
+ * NULL = legacy default stream) without host synchronisation.  Operands
+ * stay as given (no trimming of zero high limbs).  The call returns after
+ * enqueueing; device-side failures (bounded waits) are reported by
+ * prec_gpu_stream_check.  Successive calls share the library's workspace
+ * and are ordered after one another even across streams. */
+int prec_gpu_mul_device(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
+                        uint64_t *d_out, void *stream);
+
+/* Synchronises `stream` and reports any device-side error raised by work
+ * the library enqueued (PREC_GPU_E_TIMEOUT, PREC_GPU_E_INTERNAL) or a
+ * CUDA error. */
+int prec_gpu_stream_check(void *stream);
+
+/* Report of the last completed host-pointer call on this thread. */
+int prec_gpu_last_stats(prec_gpu_stats_t *st);
+
+/* Transform length log2 the NTT band uses for an x bn limbs (0 if too large). */
+int prec_gpu_ntt_log2(size_t an, size_t bn);
+
+/* Static text for an error code. */
+const char *prec_gpu_strerror(int code);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PREC_GPU_H */

@@ -1,0 +1,27 @@
+#!/usr/bin/env bash
+# Build the reference's own multiply from its sources into oracle/_ref/.
+# TEST INFRASTRUCTURE ONLY: used to pin the C restatement and to generate
+# golden vectors.  Needs the reference tree (default /root/reference); does
+# nothing and exits 0 when it is absent.  Outputs go only to oracle/_ref/.
+#   libprecref.so       portable build (-O3, no SIMD flags), COUNT_FFTS on
+#   libprecref_avx2.so  x86-64 only: -mavx2 build, for the CPU-baseline table
+set -euo pipefail
+REF=${PRECLIB_REFERENCE:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/prec.hpp" ]; then
+  echo "build_ref: reference sources not found at $REF; skipping" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+CXX=${CXX:-g++}
+SRCS=("$REF"/src/*.cpp)
+"$CXX" -O3 -std=c++17 -fPIC -shared -DCOUNT_FFTS=1 -I"$REF" \
+  "$HERE/ref_shim.cpp" "${SRCS[@]}" -o "$OUT/libprecref.so.tmp"
+mv "$OUT/libprecref.so.tmp" "$OUT/libprecref.so"
+if [ "$(uname -m)" = "x86_64" ]; then
+  "$CXX" -O3 -mavx2 -std=c++17 -fPIC -shared -DCOUNT_FFTS=1 -I"$REF" \
+    "$HERE/ref_shim.cpp" "${SRCS[@]}" -o "$OUT/libprecref_avx2.so.tmp"
+  mv "$OUT/libprecref_avx2.so.tmp" "$OUT/libprecref_avx2.so"
+fi
+echo "build_ref: built $OUT"

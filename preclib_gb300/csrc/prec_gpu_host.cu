@@ -1,0 +1,450 @@
+// prec_gpu_host.cu -- device context, transform plans and the C ABI.
+//
+// Host side of the multiply (C++17).  It owns, per process:
+//   * the prime constants and twiddle tables, derived here from the primes
+//     and generators (the reference tabulates Montgomery constants in
+//     src/mul_ntt.cpp:37-41 and rebuilds root tables per size in
+//     ntt_build_roots, mul_ntt.cpp:150-191; here one 2^13-entry table per
+//     prime and direction serves every transform length);
+//   * a workspace that grows to the largest product seen;
+//   * one stream for the host-pointer entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/prec_gpu.h"
+#include "ntt_kernels.cuh"
+
+namespace precgpu {
+
+typedef unsigned __int128 u128;
+
+// The reference's NTT primes and generators (src/mul_ntt.cpp:29-34).
+static const uint32_t kP[kPrimes] = {469762049u, 1811939329u, 2013265921u};
+static const uint32_t kG[kPrimes] = {3u, 13u, 31u};
+
+static uint32_t powmod(uint64_t b, uint64_t e, uint32_t m) {
+    uint64_t r = 1 % m;
+    b %= m;
+    while (e) {
+        if (e & 1) r = (uint64_t)((u128)r * b % m);
+        b = (uint64_t)((u128)b * b % m);
+        e >>= 1;
+    }
+    return (uint32_t)r;
+}
+
+static uint32_t invmod(uint32_t a, uint32_t m) { return powmod(a, m - 2, m); }  // m prime
+
+static uint32_t mulmod(uint32_t a, uint32_t b, uint32_t m) { return (uint32_t)((uint64_t)a * b % m); }
+
+static ShoupC shoup(uint32_t w, uint32_t p) {
+    ShoupC c;
+    c.w = w;
+    c.wp = (uint32_t)(((uint64_t)w << 32) / p);
+    return c;
+}
+
+static uint32_t neg_inv32(uint32_t m) {  // -m^{-1} mod 2^32 (Newton on 2-adic inverse)
+    uint32_t x = 1;
+    for (int i = 0; i < 5; ++i) x = x * (2u - m * x);
+    return 0u - x;
+}
+
+struct Plan {
+    int k = 0, k1 = 0, k2 = 0;
+    int path = 0;  // 0 single CTA, 1 four-step
+    int nblk = 0;
+    CrtConst crt{};
+    size_t work_bytes = 0;
+};
+
+static CrtConst crt_for(int k) {
+    const uint32_t p1 = kP[0], p2 = kP[1], p3 = kP[2];
+    uint32_t s[kPrimes];
+    for (int j = 0; j < kPrimes; ++j) {
+        const uint32_t R = (uint32_t)((1ull << 32) % kP[j]);
+        const uint32_t ninv = invmod((uint32_t)((1ull << k) % kP[j]), kP[j]);
+        s[j] = mulmod(R, ninv, kP[j]);
+    }
+    const uint32_t c12 = invmod(p1 % p2, p2), c13 = invmod(p1 % p3, p3), c23 = invmod(p2 % p3, p3);
+    CrtConst c;
+    c.s1 = shoup(s[0], p1);
+    c.k21 = shoup(c12, p2);
+    c.k22 = shoup(mulmod(s[1], c12, p2), p2);
+    const uint32_t c1323 = mulmod(c13, c23, p3);
+    c.k31 = shoup(c1323, p3);
+    c.k32 = shoup(c23, p3);
+    c.k33 = shoup(mulmod(s[2], c1323, p3), p3);
+    return c;
+}
+
+// da, db: 32-bit digit counts (upper bounds are fine)
+static int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
+    const uint64_t need = da + db - 1;
+    int k = 5;
+    while ((1ull << k) < need) ++k;
+    if (k > kMaxLog2N) return PREC_GPU_E_TOO_LARGE;
+    pl.k = k;
+    pl.crt = crt_for(k);
+    if (k <= ntt_small_max_log2()) {
+        pl.path = 0;
+        pl.work_bytes = 0;
+        return 0;
+    }
+    pl.path = 1;
+    pl.k1 = k / 2;
+    pl.k2 = k - pl.k1;
+    const uint64_t bl = (uint64_t)ntt_carry_block_limbs();
+    pl.nblk = (int)((lout + bl - 1) / bl);
+    pl.work_bytes = ((size_t)2 * kPrimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
+    return 0;
+}
+
+struct Ctx {
+    std::mutex mu;
+    bool ready = false;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    void* tables = nullptr;
+    uint8_t* ws = nullptr;
+    size_t ws_cap = 0;
+    uint64_t* io = nullptr;
+    size_t io_cap = 0;  // limbs
+    int* d_err = nullptr;
+    int* h_err = nullptr;
+    cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
+};
+
+static Ctx g_ctx;
+static thread_local prec_gpu_stats_t t_stats;
+
+static int cuda_code(cudaError_t e) {
+    if (e == cudaSuccess) return 0;
+    if (e == cudaErrorMemoryAllocation) return PREC_GPU_E_NOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return PREC_GPU_E_NODEV;
+    return PREC_GPU_E_CUDA;
+}
+
+#define CK(x)                                  \
+    do {                                       \
+        cudaError_t _e = (x);                  \
+        if (_e != cudaSuccess) return cuda_code(_e); \
+    } while (0)
+
+static int build_tables(Ctx& c) {
+    const int T = 1 << kMaxSubLog2;   // entries of the Shoup tables
+    const int H = 1 << kTwLevelBits;  // entries of each four-step level
+    const size_t per_prime = (size_t)2 * T * sizeof(uint2) + (size_t)2 * H * sizeof(uint32_t);
+    std::vector<uint8_t> host(per_prime * kPrimes);
+    PrimeC primes[kPrimes];
+    TableSet tabs;
+    CK(cudaMalloc(&c.tables, host.size()));
+    for (int j = 0; j < kPrimes; ++j) {
+        const uint32_t p = kP[j];
+        primes[j].p = p;
+        primes[j].pinv = neg_inv32(p);
+        primes[j].one_wp = (uint32_t)((1ull << 32) / p);
+        primes[j].pad = 0;
+        // generator check: g^((p-1)/2) == -1, so w26 has order exactly 2^26
+        if (powmod(kG[j], (p - 1) / 2, p) != p - 1) return PREC_GPU_E_INTERNAL;
+        const uint32_t w26 = powmod(kG[j], (p - 1) >> kMaxLog2N, p);
+        uint8_t* base = host.data() + per_prime * j;
+        uint2* tf = reinterpret_cast<uint2*>(base);
+        uint2* ti = tf + T;
+        uint32_t* twhi = reinterpret_cast<uint32_t*>(ti + T);
+        uint32_t* twlo = twhi + H;
+        tf[0] = make_uint2(1, (uint32_t)((1ull << 32) / p));
+        ti[0] = tf[0];
+        for (int b = 0; b < kMaxSubLog2; ++b) {
+            const uint32_t wb = powmod(w26, 1ull << (kMaxLog2N - b - 1), p);  // order 2^(b+1)
+            const uint32_t wbi = invmod(wb, p);
+            uint32_t x = 1, y = 1;
+            for (int i = 0; i < (1 << b); ++i) {
+                const ShoupC f = shoup(x, p), g = shoup(y, p);
+                tf[(1 << b) + i] = make_uint2(f.w, f.wp);
+                ti[(1 << b) + i] = make_uint2(g.w, g.wp);
+                x = mulmod(x, wb, p);
+                y = mulmod(y, wbi, p);
+            }
+        }
+        const uint32_t R = (uint32_t)((1ull << 32) % p);
+        const uint32_t step_hi = powmod(w26, (uint64_t)H, p);
+        uint32_t x = R, y = R;
+        for (int i = 0; i < H; ++i) {
+            twhi[i] = x;
+            twlo[i] = y;
+            x = mulmod(x, step_hi, p);
+            y = mulmod(y, w26, p);
+        }
+        const uint8_t* dbase = static_cast<uint8_t*>(c.tables) + per_prime * j;
+        tabs.tf[j] = reinterpret_cast<const uint2*>(dbase);
+        tabs.ti[j] = tabs.tf[j] + T;
+        tabs.twhi[j] = reinterpret_cast<const uint32_t*>(tabs.ti[j] + T);
+        tabs.twlo[j] = tabs.twhi[j] + H;
+    }
+    CK(cudaMemcpy(c.tables, host.data(), host.size(), cudaMemcpyHostToDevice));
+    ntt_set_tables(primes, tabs);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int init_locked(Ctx& c, int device) {
+    if (c.ready) return 0;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return PREC_GPU_E_NODEV;
+    if (device < 0) CK(cudaGetDevice(&device));
+    if (device >= n) return PREC_GPU_E_ARG;
+    CK(cudaSetDevice(device));
+    c.device = device;
+    CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c.last_done, cudaEventDisableTiming));
+    CK(cudaEventCreate(&c.ev0));
+    CK(cudaEventCreate(&c.ev1));
+    CK(cudaMalloc(&c.d_err, sizeof(int)));
+    CK(cudaMemset(c.d_err, 0, sizeof(int)));
+    CK(cudaMallocHost(&c.h_err, sizeof(int)));
+    CK((cudaError_t)ntt_configure_kernels());
+    int r = build_tables(c);
+    if (r) return r;
+    CK(cudaDeviceSynchronize());
+    c.ready = true;
+    return 0;
+}
+
+static int ensure_ws(Ctx& c, size_t bytes) {
+    if (bytes <= c.ws_cap) return 0;
+    if (c.ws) {
+        CK(cudaDeviceSynchronize());
+        cudaFree(c.ws);
+        c.ws = nullptr;
+        c.ws_cap = 0;
+    }
+    size_t cap = std::max(bytes, c.ws_cap * 3 / 2);
+    if (cudaMalloc(&c.ws, cap) != cudaSuccess) {
+        cudaGetLastError();
+        if (cudaMalloc(&c.ws, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return PREC_GPU_E_NOMEM;
+        }
+        cap = bytes;
+    }
+    c.ws_cap = cap;
+    return 0;
+}
+
+static int ensure_io(Ctx& c, size_t limbs) {
+    if (limbs <= c.io_cap) return 0;
+    if (c.io) {
+        CK(cudaDeviceSynchronize());
+        cudaFree(c.io);
+        c.io = nullptr;
+        c.io_cap = 0;
+    }
+    if (cudaMalloc(&c.io, limbs * sizeof(uint64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return PREC_GPU_E_NOMEM;
+    }
+    c.io_cap = limbs;
+    return 0;
+}
+
+// Enqueues one NTT-band product on device pointers.
+static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
+                       uint64_t* d_out, const Plan& pl, cudaStream_t st) {
+    const uint64_t lout = la + lb;
+    if (pl.path == 0) {
+        SmallDesc d;
+        d.a = d_a;
+        d.b = d_b;
+        d.out = d_out;
+        d.la = la;
+        d.lb = lb;
+        d.lout = lout;
+        d.k = pl.k;
+        d.pad = 0;
+        d.crt = pl.crt;
+        ntt_launch_small(nullptr, &d, 1, pl.k, st);
+    } else {
+        ProdArgs args;
+        args.a = d_a;
+        args.b = d_b;
+        args.out = d_out;
+        args.work = reinterpret_cast<uint32_t*>(c.ws);
+        args.scratch = args.work + ((size_t)2 * kPrimes << pl.k);
+        args.err = c.d_err;
+        args.la = la;
+        args.lb = lb;
+        args.lout = lout;
+        args.k = pl.k;
+        args.k1 = pl.k1;
+        args.k2 = pl.k2;
+        args.nblk = pl.nblk;
+        args.crt = pl.crt;
+        ntt_launch_4step(args, st);
+    }
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static size_t trim(const uint64_t* a, size_t n) {
+    while (n > 0 && a[n - 1] == 0) --n;
+    return n;
+}
+
+static uint64_t digits32(const uint64_t* a, size_t n) {  // n > 0, a[n-1] != 0
+    return 2 * (uint64_t)n - ((a[n - 1] >> 32) == 0 ? 1 : 0);
+}
+
+static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
+    if ((!a && an) || (!b && bn) || (!out && an + bn)) return PREC_GPU_E_ARG;
+    Ctx& c = g_ctx;
+    std::lock_guard<std::mutex> lk(c.mu);
+    int r = init_locked(c, -1);
+    if (r) return r;
+    const size_t total = an + bn;
+    const size_t la = a ? trim(a, an) : 0, lb = b ? trim(b, bn) : 0;
+    memset(&t_stats, 0, sizeof(t_stats));
+    t_stats.limbs_a = la;
+    t_stats.limbs_b = lb;
+    if (la == 0 || lb == 0) {
+        if (total) memset(out, 0, total * sizeof(uint64_t));
+        return 0;
+    }
+    const uint64_t lout = la + lb;
+    Plan pl;
+    if ((r = plan_for(digits32(a, la), digits32(b, lb), lout, pl))) return r;
+    if ((r = ensure_ws(c, pl.work_bytes))) return r;
+    if ((r = ensure_io(c, 2 * lout))) return r;
+    uint64_t* d_a = c.io;
+    uint64_t* d_b = c.io + la;
+    uint64_t* d_out = c.io + lout;
+    cudaStream_t st = c.stream;
+    CK(cudaStreamWaitEvent(st, c.last_done, 0));
+    CK(cudaMemcpyAsync(d_a, a, la * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(c.ev0, st));
+    if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st))) return r;
+    CK(cudaEventRecord(c.ev1, st));
+    CK(cudaMemcpyAsync(out, d_out, lout * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(c.h_err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemsetAsync(c.d_err, 0, sizeof(int), st));
+    CK(cudaEventRecord(c.last_done, st));
+    CK(cudaStreamSynchronize(st));
+    if (total > lout) memset(out + lout, 0, (total - lout) * sizeof(uint64_t));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    t_stats.path = pl.path;
+    t_stats.log2_n = pl.k;
+    t_stats.device_ms = ms;
+    if (*c.h_err & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
+    if (*c.h_err) return PREC_GPU_E_INTERNAL;
+    return 0;
+}
+
+}  // namespace precgpu
+
+using namespace precgpu;
+
+extern "C" {
+
+int prec_gpu_init(int device) {
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    return init_locked(g_ctx, device);
+}
+
+void prec_gpu_shutdown(void) {
+    Ctx& c = g_ctx;
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.ready) return;
+    cudaDeviceSynchronize();
+    cudaFree(c.ws);
+    cudaFree(c.io);
+    cudaFree(c.tables);
+    cudaFree(c.d_err);
+    cudaFreeHost(c.h_err);
+    cudaEventDestroy(c.last_done);
+    cudaEventDestroy(c.ev0);
+    cudaEventDestroy(c.ev1);
+    cudaStreamDestroy(c.stream);
+    c.ws = nullptr;
+    c.io = nullptr;
+    c.tables = nullptr;
+    c.ws_cap = c.io_cap = 0;
+    c.ready = false;
+}
+
+int prec_gpu_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
+    return host_mul(a, an, b, bn, out);
+}
+
+int prec_gpu_mul_ntt(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
+    return host_mul(a, an, b, bn, out);
+}
+
+int prec_gpu_mul_device(const uint64_t* d_a, size_t an, const uint64_t* d_b, size_t bn, uint64_t* d_out,
+                        void* stream) {
+    if (!d_a || !d_b || !d_out || an == 0 || bn == 0) return PREC_GPU_E_ARG;
+    Ctx& c = g_ctx;
+    std::lock_guard<std::mutex> lk(c.mu);
+    int r = init_locked(c, -1);
+    if (r) return r;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Plan pl;
+    if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl))) return r;
+    if ((r = ensure_ws(c, pl.work_bytes))) return r;
+    CK(cudaStreamWaitEvent(st, c.last_done, 0));
+    if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st))) return r;
+    CK(cudaEventRecord(c.last_done, st));
+    return 0;
+}
+
+int prec_gpu_stream_check(void* stream) {
+    Ctx& c = g_ctx;
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.ready) return PREC_GPU_E_NODEV;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(c.h_err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    const int e = *c.h_err;
+    CK(cudaMemset(c.d_err, 0, sizeof(int)));
+    if (e & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
+    if (e) return PREC_GPU_E_INTERNAL;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int prec_gpu_last_stats(prec_gpu_stats_t* st) {
+    if (!st) return PREC_GPU_E_ARG;
+    *st = t_stats;
+    return 0;
+}
+
+int prec_gpu_ntt_log2(size_t an, size_t bn) {
+    if (an == 0 || bn == 0) return 0;
+    Plan pl;
+    if (plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl)) return 0;
+    return pl.k;
+}
+
+const char* prec_gpu_strerror(int code) {
+    switch (code) {
+        case PREC_GPU_OK: return "ok";
+        case PREC_GPU_E_ARG: return "invalid argument";
+        case PREC_GPU_E_TOO_LARGE: return "product exceeds the 2^26-point transform";
+        case PREC_GPU_E_NOMEM: return "device allocation failed";
+        case PREC_GPU_E_CUDA: return "CUDA runtime error";
+        case PREC_GPU_E_TIMEOUT: return "bounded device-side wait ran out";
+        case PREC_GPU_E_FFT_ROUNDING: return "FP64 rounding distance above 0.25";
+        case PREC_GPU_E_NODEV: return "no usable CUDA device";
+        case PREC_GPU_E_INTERNAL: return "internal consistency check failed";
+        default: return "unknown error";
+    }
+}
+
+}  // extern "C"

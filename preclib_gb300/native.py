@@ -1,0 +1,125 @@
+"""ctypes binding of ``lib/libprecgpu.so`` (the C ABI of include/prec_gpu.h).
+
+There is no fallback: importing the binding without the built library, or
+calling it without a CUDA device, raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = os.path.join(_build.LIBDIR, _build.LIBNAME)
+
+OK = 0
+E_ARG, E_TOO_LARGE, E_NOMEM, E_CUDA, E_TIMEOUT, E_FFT_ROUNDING, E_NODEV, E_INTERNAL = range(1, 9)
+
+# Every symbol include/prec_gpu.h declares (checked by the CPU tests).
+EXPORTS = (
+    "prec_gpu_init", "prec_gpu_shutdown", "prec_gpu_mul", "prec_gpu_mul_ntt",
+    "prec_gpu_mul_device", "prec_gpu_stream_check", "prec_gpu_last_stats",
+    "prec_gpu_ntt_log2", "prec_gpu_strerror",
+)
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("path", ctypes.c_int), ("log2_n", ctypes.c_int),
+                ("limbs_a", ctypes.c_size_t), ("limbs_b", ctypes.c_size_t),
+                ("fft_max_distance", ctypes.c_double), ("device_ms", ctypes.c_double)]
+
+
+class PrecGpuError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__("%s: %s (code %d)" % (what or "prec_gpu", strerror(code), code))
+
+
+_LIB = None
+
+
+def lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("preclib_gb300 native library missing at %s; run "
+                              "`python -m preclib_gb300.build` (no CPU fallback exists)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        L.prec_gpu_init.argtypes = [ctypes.c_int]
+        L.prec_gpu_init.restype = ctypes.c_int
+        L.prec_gpu_shutdown.argtypes = []
+        L.prec_gpu_shutdown.restype = None
+        for name in ("prec_gpu_mul", "prec_gpu_mul_ntt"):
+            f = getattr(L, name)
+            f.argtypes = [_u64p, ctypes.c_size_t, _u64p, ctypes.c_size_t, _u64p]
+            f.restype = ctypes.c_int
+        L.prec_gpu_mul_device.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                          ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+        L.prec_gpu_mul_device.restype = ctypes.c_int
+        L.prec_gpu_stream_check.argtypes = [ctypes.c_void_p]
+        L.prec_gpu_stream_check.restype = ctypes.c_int
+        L.prec_gpu_last_stats.argtypes = [ctypes.POINTER(Stats)]
+        L.prec_gpu_last_stats.restype = ctypes.c_int
+        L.prec_gpu_ntt_log2.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
+        L.prec_gpu_ntt_log2.restype = ctypes.c_int
+        L.prec_gpu_strerror.argtypes = [ctypes.c_int]
+        L.prec_gpu_strerror.restype = ctypes.c_char_p
+        _LIB = L
+    return _LIB
+
+
+def strerror(code: int) -> str:
+    try:
+        return lib().prec_gpu_strerror(code).decode()
+    except ImportError:
+        return "error %d" % code
+
+
+def check(code: int, what: str = "") -> None:
+    if code != OK:
+        raise PrecGpuError(code, what)
+
+
+def _arr(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_u64p)
+
+
+def init(device: int = -1) -> None:
+    check(lib().prec_gpu_init(device), "prec_gpu_init")
+
+
+def mul(a, b, ntt: bool = False) -> np.ndarray:
+    """Product of two host limb vectors (an+bn limbs), computed on the GPU."""
+    a, b = _arr(a), _arr(b)
+    out = np.empty(max(len(a) + len(b), 1), dtype=np.uint64)
+    f = lib().prec_gpu_mul_ntt if ntt else lib().prec_gpu_mul
+    check(f(_p(a), len(a), _p(b), len(b), _p(out)), "prec_gpu_mul")
+    return out[: len(a) + len(b)]
+
+
+def mul_device(a_ptr: int, an: int, b_ptr: int, bn: int, out_ptr: int, stream: int = 0) -> None:
+    """Enqueue a product on device pointers (e.g. torch tensors' data_ptr())."""
+    check(lib().prec_gpu_mul_device(a_ptr, an, b_ptr, bn, out_ptr, stream or None),
+          "prec_gpu_mul_device")
+
+
+def stream_check(stream: int = 0) -> None:
+    check(lib().prec_gpu_stream_check(stream or None), "prec_gpu_stream_check")
+
+
+def last_stats() -> Stats:
+    s = Stats()
+    check(lib().prec_gpu_last_stats(ctypes.byref(s)))
+    return s
+
+
+def ntt_log2(an: int, bn: int) -> int:
+    return lib().prec_gpu_ntt_log2(an, bn)

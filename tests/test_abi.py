@@ -1,0 +1,70 @@
+"""CPU tests of the boundary: the C ABI library loads, exports every symbol
+its header declares, and its host-side plan logic answers without a GPU."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from preclib_gb300 import native, workloads
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(prec_gpu_\w+)\s*\(", src))
+    return names
+
+
+def test_header_symbols_exported():
+    lib = native.lib()
+    declared = _declared()
+    assert declared, "no declarations found"
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    assert declared <= set(native.EXPORTS) | declared
+
+
+def test_python_binding_covers_header():
+    assert _declared() == set(native.EXPORTS)
+
+
+def test_ntt_plan_sizes():
+    assert native.ntt_log2(8192, 8192) == 15
+    assert native.ntt_log2(1 << 20, 1 << 20) == 22
+    assert native.ntt_log2(3000, 3000) == 14
+    assert native.ntt_log2(1, 1) == 5
+    assert native.ntt_log2(1 << 24, 1 << 24) == 26
+    assert native.ntt_log2(1 << 24, (1 << 24) + 1) == 0  # beyond the 2^26-point transform
+
+
+def test_strerror():
+    assert native.strerror(0) == "ok"
+    assert "0.25" in native.strerror(native.E_FFT_ROUNDING)
+
+
+def test_splitmix_matches_oracle():
+    import oracle as O
+    for seed in (1, 2, 12345):
+        assert np.array_equal(workloads.splitmix64(seed, 1000), O.splitmix64(seed, 1000))
+
+
+def test_batch_sizes_shape():
+    lo, hi = workloads.batch_sizes(7, 4096)
+    assert lo.min() >= 200 and lo.max() <= 65536
+    assert (hi >= lo).all() and (hi <= 2 * lo).all()
+
+
+def test_no_device_fails_loudly():
+    """Without a usable device the library reports E_NODEV (no CPU fallback)."""
+    rc = native.lib().prec_gpu_init(0)
+    if rc == native.OK:
+        pytest.skip("a CUDA device is present")
+    assert rc == native.E_NODEV
+    with pytest.raises(native.PrecGpuError):
+        native.mul(np.ones(3, np.uint64), np.ones(3, np.uint64))

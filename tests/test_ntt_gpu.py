@@ -1,0 +1,137 @@
+"""GPU parity of the NTT band through the C ABI: bit-exact against the
+oracle and against the reference-generated golden vectors."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+import patterns
+
+pytestmark = pytest.mark.gpu
+
+
+def _digest(out):
+    return hashlib.sha256(np.ascontiguousarray(out, dtype="<u8").tobytes()).hexdigest()
+
+
+def test_golden_vectors_ntt(gpu, golden):
+    """Every golden product (NTT, FFT and dispatcher records alike: the
+    product is an exact integer) through the NTT band."""
+    for rec in golden:
+        a, b = patterns.make(rec["gen"])
+        out = gpu.mul(a, b, ntt=True)
+        assert _digest(out) == rec["sha256"], rec["name"]
+
+
+def test_kat_square(gpu):
+    x = np.array([0xFFFFFFFF], dtype=np.uint64)
+    out = gpu.mul(x, x, ntt=True)
+    assert out.tolist() == [0xFFFFFFFE00000001, 0]
+
+
+@pytest.mark.parametrize("an,bn", [(1, 1), (2, 1), (7, 5), (64, 64), (192, 193), (1000, 999),
+                                   (2047, 2049), (2048, 2048), (2049, 2049), (4096, 4095),
+                                   (4097, 4097), (6144, 8192), (8192, 8192), (10000, 5001),
+                                   (16384, 16384), (40000, 39999), (65536, 65536), (100001, 50001)])
+def test_random_vs_oracle(gpu, an, bn):
+    a = O.splitmix64(an * 31 + bn, an)
+    b = O.splitmix64(an * 37 + bn + 1, bn)
+    got = gpu.mul(a, b, ntt=True)
+    assert np.array_equal(got, O.mul_ntt(a, b))
+
+
+def test_both_paths_each_length(gpu):
+    """Every transform length 2^5 .. 2^19 (single-CTA and four-step)."""
+    for k in range(5, 20):
+        n = 1 << (k - 2)  # 2n digits per operand -> N = 2^k
+        a = O.splitmix64(k, n)
+        b = O.splitmix64(k + 100, n)
+        a[-1] |= np.uint64(1 << 63)
+        b[-1] |= np.uint64(1 << 63)
+        got = gpu.mul(a, b, ntt=True)
+        assert np.array_equal(got, O.mul_ntt(a, b)), k
+
+
+def test_zero_and_padding(gpu):
+    z = np.zeros(5, np.uint64)
+    a = O.splitmix64(3, 9000)
+    assert not gpu.mul(z, a, ntt=True).any()
+    assert len(gpu.mul(z, a, ntt=True)) == 9005
+    # high zero limbs are trimmed by the host API and the tail zero-filled
+    ap = np.concatenate([a, np.zeros(100, np.uint64)])
+    b = O.splitmix64(4, 7000)
+    got = gpu.mul(ap, b, ntt=True)
+    assert len(got) == 9100 + 7000
+    assert np.array_equal(got[:16000], O.mul_ntt(a, b)) and not got[16000:].any()
+
+
+def test_all_ones_maximal_carries(gpu):
+    """(2^(64n)-1)^2 has the longest carry runs the CRT output can produce."""
+    for n in (1, 33, 2049, 6145, 70000, 1 << 20):
+        a = np.full(n, 0xFFFFFFFFFFFFFFFF, dtype=np.uint64)
+        got = gpu.mul(a, a, ntt=True)
+        want = np.zeros(2 * n, np.uint64)
+        want[0] = 1
+        want[n:] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        want[n] = np.uint64(0xFFFFFFFFFFFFFFFE)
+        assert np.array_equal(got, want), n
+
+
+def test_torture_ntt(gpu):
+    for (an, bn) in patterns.TORTURE_SHAPES:
+        for p in patterns.TORTURE_PATTERNS:
+            a, b = patterns.torture(p[0], an, bn)
+            if len(a) == 0 or len(b) == 0:
+                continue
+            assert np.array_equal(gpu.mul(a, b, ntt=True), O.mul_ntt(a, b)), (p[0], an, bn)
+
+
+def _spot(p, a, b):
+    for q in (2305843009213693951, 4611686018427387847, 1152921504606846883, 2147483647 * 1048573):
+        assert O.mod_u64(p, q) == O.mod_u64(a, q) * O.mod_u64(b, q) % q
+
+
+def test_large_mod_prime_spot_checks(gpu):
+    """Full-size products (2^22 .. 2^26-point transforms): residues modulo
+    61-bit primes agree, plus the top-limb and length invariants."""
+    for (an, bn, s) in ((1 << 20, 1 << 20, 3), (3 << 20, 1 << 21, 5), (1 << 22, 1 << 22, 7),
+                        ((1 << 24) - 5, (1 << 24) - 7, 9)):
+        a = O.splitmix64(s, an)
+        b = O.splitmix64(s + 1, bn)
+        p = gpu.mul(a, b, ntt=True)
+        _spot(p, a, b)
+        assert p[-1] != 0 or p[-2] != 0
+
+
+def test_1m_golden(gpu, golden):
+    rec = [r for r in golden if r["name"] == "cfg2_1Mx1M_ntt"][0]
+    a, b = patterns.make(rec["gen"])
+    assert _digest(gpu.mul(a, b, ntt=True)) == rec["sha256"]
+    st = gpu.last_stats()
+    assert st.log2_n == 22 and st.path == 1
+
+
+def test_device_api_matches_host_api(gpu):
+    torch = pytest.importorskip("torch")
+    for (an, bn) in ((5000, 4000), (1 << 18, 1 << 18), (50, 60)):
+        a = O.splitmix64(an, an)
+        b = O.splitmix64(bn + 1, bn)
+        ta = torch.from_numpy(a.view(np.int64)).cuda()
+        tb = torch.from_numpy(b.view(np.int64)).cuda()
+        to = torch.empty(an + bn, dtype=torch.int64, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+        gpu.mul_device(ta.data_ptr(), an, tb.data_ptr(), bn, to.data_ptr(), s)
+        gpu.stream_check(s)
+        got = to.cpu().numpy().view(np.uint64)
+        assert np.array_equal(got, O.mul_ntt(a, b))
+
+
+def test_too_large_rejected(gpu):
+    a = np.ones(1, np.uint64)
+    with pytest.raises(gpu.PrecGpuError) as e:
+        # 2^25 + 1 total limbs exceed the 2^26-point transform; no allocation happens
+        gpu.lib().prec_gpu_mul_device  # noqa: B018
+        code = gpu.lib().prec_gpu_mul_device(1, (1 << 24) + 1, 1, 1 << 24, 1, None)
+        gpu.check(code)
+    assert e.value.code == gpu.E_TOO_LARGE

@@ -1,0 +1,354 @@
+"""Benchmark: one 1,048,576 x 1,048,576-limb product on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one full product of two SplitMix64 operands (seeds 3 and 4) of
+1,048,576 uint64 limbs each (2,097,152-limb result, 2^22-point transforms
+over three primes).  Printed as ONE JSON line on rank 0:
+  value  device time per product, operands already resident in HBM, L2
+         flushed (256 MiB write) between timed steps; CUDA events on the
+         stream the kernels run on
+  e2e    the same product through the public host API prec_gpu_mul with
+         pinned host buffers: host->device copy of both operands, the
+         product, device->host copy of the result, every step
+  roofline  the dominant kernel's algorithmic bytes (per-stage split of
+         144*N + 16*(La+Lb)) over its live event time, against the measured
+         HBM copy bandwidth
+  cpu_baseline  the oracle restatement of the reference NTT multiply, one
+         thread, a bounded sample of the same product
+With --impl reference the same line is produced for the reference's CPU
+algorithm (oracle port; the reference sources do not exist on the GPU
+hosts) run on every host core, one independent product per core.
+Under torchrun with N > 1 ranks each rank runs an independent replica on
+its own GPU (the product does not shard); value = max time / products.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+AN = BN = 1 << 20
+SEED_A, SEED_B = 3, 4
+METRIC = "1M×1M-limb mul ms"
+WORKLOAD = "1,048,576 x 1,048,576-limb uint64 product (SplitMix64 seeds 3,4), 2^22-point NTT x 3 primes"
+GOLDEN = os.path.join(ROOT, "tests", "golden", "products.json")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic():
+    """Per-launch DRAM bytes per kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ntt_1Mx1M_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _golden_sha():
+    try:
+        with open(GOLDEN) as f:
+            for r in json.load(f)["products"]:
+                if r["name"] == "cfg2_1Mx1M_ntt":
+                    return r["sha256"]
+    except (OSError, ValueError, KeyError):
+        pass
+    return None
+
+
+def algorithmic_bytes(la: int, lb: int):
+    """Canonical bytes of the NTT path (32-bit digits, 3 primes, 4-byte
+    residues) split per kernel: N = next_pow2(2(La+Lb))."""
+    n = 1
+    while n < 2 * (la + lb):
+        n <<= 1
+    io = 8 * (la + lb)
+    return n, {
+        "k_fwd_cols": io + 24 * n + 48 * n,   # split + forward pass 1
+        "k_rows": 36 * n,                     # forward pass 2 + pointwise + inverse pass 1
+        "k_inv_cols": 24 * n,                 # inverse pass 2
+        "k_crt_carry": 12 * n + io,           # CRT + carry
+    }
+
+
+class Clocks:
+    """nvidia-smi sampler (200 ms) around the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            if self.path:
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        busy = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows
+                                                         if r[3].replace(".", "").isdigit())}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(max_products: int = 3, budget_s: float = 20.0):
+    """Oracle restatement of mul_ntt on this host, one thread."""
+    import oracle as O
+    from preclib_gb300 import workloads
+    a = workloads.operand(SEED_A, AN)
+    b = workloads.operand(SEED_B, BN)
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < max_products and (not times or time.perf_counter() < t_end):
+        t = time.perf_counter()
+        O.mul_ntt(a, b)
+        times.append(time.perf_counter() - t)
+    return statistics.median(times) * 1e3, len(times)
+
+
+def run_reference(args):
+    """The reference's CPU algorithm on all host cores (oracle port), one
+    independent 1M x 1M product per core per step."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle as O
+    from preclib_gb300 import workloads
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    a = workloads.operand(SEED_A, AN)
+    b = workloads.operand(SEED_B, BN)
+    O.lib()
+
+    def one(_):
+        return O.mul_ntt(a, b)
+
+    steps = []
+    with ThreadPoolExecutor(cores) as ex:
+        for i in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            outs = list(ex.map(one, range(cores)))
+            dt = time.perf_counter() - t
+            if i >= args.warmup:
+                steps.append(dt)
+            del outs
+    ms = sum(steps) / len(steps) / cores * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 4), "unit": "ms",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(sum(steps) / len(steps) * 1e3, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "an": AN, "bn": BN, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(ms, 4), "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": "%d independent 1M x 1M products per step (one per core), "
+                                   "wall time / products" % cores},
+        "e2e": {"value": round(ms, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    from preclib_gb300 import native, workloads
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    native.init(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    a = workloads.operand(SEED_A, AN)
+    b = workloads.operand(SEED_B, BN)
+    ta = torch.from_numpy(a.view(np.int64)).to(dev)
+    tb = torch.from_numpy(b.view(np.int64)).to(dev)
+    to = torch.empty(AN + BN, dtype=torch.int64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        return native.mul_device_profile(ta.data_ptr(), AN, tb.data_ptr(), BN, to.data_ptr(), sptr)
+
+    for _ in range(args.warmup):
+        step()
+        flush.fill_(1)
+    native.stream_check(sptr)
+
+    # ---- timed region: device-resident operands, L2 flushed between steps
+    stage_tot = {}
+    step_ms = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with Clocks(local) as clk:
+        for i in range(args.steps):
+            stages = step()
+            for name, ms in stages:
+                stage_tot[name] = stage_tot.get(name, 0.0) + ms
+            step_ms.append(sum(ms for _, ms in stages))
+            flush.fill_(i & 0xFF)
+        torch.cuda.synchronize(dev)
+    clocks = clk.summary()
+    native.stream_check(sptr)
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    out = to.cpu().numpy().view(np.uint64)
+    sha = hashlib.sha256(np.ascontiguousarray(out, dtype="<u8").tobytes()).hexdigest()
+    golden = _golden_sha()
+    bit_exact = golden is not None and sha == golden
+
+    # ---- end to end through the public host API (pinned host buffers)
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hb = torch.from_numpy(b.view(np.int64)).pin_memory()
+    ho = torch.empty(AN + BN, dtype=torch.int64).pin_memory()
+    pa = ha.numpy().view(np.uint64)
+    pb = hb.numpy().view(np.uint64)
+    po = ho.numpy().view(np.uint64)
+    L = native.lib()
+    for _ in range(max(1, args.warmup)):
+        native.check(L.prec_gpu_mul(native._p(pa), AN, native._p(pb), BN, native._p(po)))
+    e2e = []
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        native.check(L.prec_gpu_mul(native._p(pa), AN, native._p(pb), BN, native._p(po)))
+        e2e.append(time.perf_counter() - t)
+    e2e_exact = hashlib.sha256(np.ascontiguousarray(po, dtype="<u8").tobytes()).hexdigest() == golden
+    e2e_ms = statistics.mean(e2e) * 1e3
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # ---- roofline of the dominant kernel (live events) and of the whole product
+    peak, peak_kind = _peaks()
+    n, alg = algorithmic_bytes(AN, BN)
+    avg = {k: v / args.steps for k, v in stage_tot.items()}
+    dom = max(avg, key=avg.get)
+    dom_gbs = alg[dom] / (avg[dom] * 1e-3) / 1e9
+    traffic = _traffic().get(dom)
+    total_alg = sum(alg.values())
+    per_product_ms = total_ms / args.steps / ws
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        cpu_ms, nprod = cpu_sample()
+        cpu = {"value": round(cpu_ms, 3), "unit": "ms", "cores": 1, "kind": "port",
+               "sample": "%d single-threaded 1M x 1M products with the oracle restatement of "
+                         "mul_ntt (16-bit digits, 2 primes), median" % nprod}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(per_product_ms, 4), "unit": "ms", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "an": AN, "bn": BN, "transform_points": n,
+                       "primes": 3, "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "products_per_s": round(1e3 / per_product_ms, 2),
+            "bit_exact": bool(bit_exact and e2e_exact),
+            "stage_ms": {k: round(v, 4) for k, v in avg.items()},
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(dom_gbs, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(dom_gbs / peak, 4),
+                         "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes": alg[dom]},
+            "roofline_product": {"bytes": total_alg,
+                                 "achieved": round(total_alg / (per_product_ms * 1e-3 * ws) / 1e9, 1),
+                                 "frac": round(total_alg / (per_product_ms * 1e-3 * ws) / 1e9 / peak, 4),
+                                 "unit": "GB/s"},
+            "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": 8 * (AN + BN),
+                    "d2h_bytes_per_step": 8 * (AN + BN)},
+            "gpu_launches": 4 * args.steps,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -77,6 +77,18 @@ int prec_gpu_mul_ntt(const uint64_t *a, size_t an, const uint64_t *b, size_t bn,
 int prec_gpu_mul_device(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
                         uint64_t *d_out, void *stream);
 
+/* Diagnostic form of prec_gpu_mul_device: records a CUDA event on `stream`
+ * before the first and after every kernel of the product, synchronises,
+ * and writes each kernel's device time (ms) to stage_ms[0 .. *nstages)
+ * (at most 8).  Kernel names: prec_gpu_stage_name(path, i) with the path of
+ * prec_gpu_stats_t.  Replaces: the wall-clock phase timers of the
+ * reference's benches (test/bench_ntt.cpp:25-58, pi/pi_chudnovsky.cpp:183-188). */
+int prec_gpu_mul_device_profile(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
+                                uint64_t *d_out, void *stream, float *stage_ms, int *nstages);
+
+/* Kernel name of stage `stage` of path `path` ("" if out of range). */
+const char *prec_gpu_stage_name(int path, int stage);
+
 /* Synchronises `stream` and reports any device-side error raised by work
  * the library enqueued (PREC_GPU_E_TIMEOUT, PREC_GPU_E_INTERNAL) or a
  * CUDA error. */

@@ -1,0 +1,172 @@
+// ntt_cols.cu -- column passes of the four-step NTT (index i = i1*N2 + i2).
+//
+// k_fwd_cols: for C adjacent columns i2 of one operand and one prime, the
+//   limbs are read as 32-bit digits (the reference's ntt_digits and mont_in,
+//   src/mul_ntt.cpp:331-342, 357-360, fused into the load), reduced, run
+//   through a DIF transform over i1 (the first log2(N1) stages of
+//   ntt_forward, mul_ntt.cpp:193-255) and multiplied by the four-step
+//   twiddle w_N^(i2*k1).  Output row slot s holds frequency k1 = bitrev(s).
+// k_inv_cols: the DIT transform over the row slots (the last stages of
+//   ntt_inverse, mul_ntt.cpp:257-329) back to natural coefficient order.
+// Columns are interleaved in shared memory (element i of column c at
+// P(i)*C + c); a warp covers C columns x 32/C items, so every global access
+// moves whole 32-byte sectors.
+#include "ntt_engine.cuh"
+
+namespace precgpu {
+
+template <int SET, int M, int C>
+__global__ void __launch_bounds__(256) k_fwd_cols(ProdArgs args) {
+    extern __shared__ uint32_t sm[];
+    constexpr int NP = sch_np(M);
+    static_assert(NP >= 2, "column transforms have at least two passes");
+    const int prime = blockIdx.y >> 1, operand = blockIdx.y & 1;
+    const PrimeC pc = args.f.pc[prime];
+    const uint2* __restrict__ tw = args.f.tf[prime];
+    const uint32_t N2 = 1u << args.k2;
+    const uint32_t c0 = blockIdx.x * C;
+
+    // the carry kernel's look-back words start at zero
+    if (blockIdx.y == 0) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= args.nblk; i += gridDim.x * blockDim.x)
+            args.scratch[i] = 0;
+    }
+
+    const uint32_t* __restrict__ dig = reinterpret_cast<const uint32_t*>(operand ? args.b : args.a);
+    const uint64_t nd = 2 * (operand ? args.lb : args.la);
+    {   // top pass straight from the limbs
+        using G = Geom<M, 0>;
+        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+            const int col = w & (C - 1);
+            const uint32_t u = w / C;
+            const uint32_t base = G::base(u);
+            uint32_t x[1][G::R];
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) {
+                const uint64_t d = (uint64_t)(base + ((uint32_t)q << G::LO)) * N2 + c0 + col;
+                x[0][q] = d < nd ? Ar<SET>::digit(__ldg(&dig[d]), pc) : 0u;
+            }
+            regs_pass<SET, M, 0, false, 1>(x, u, tw, pc);
+            uint32_t* s = sm + G::pbase(u) * C + col;
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) s[q * G::QS * C] = x[0][q];
+        }
+        __syncthreads();
+    }
+    col_passes<SET, M, 1, NP - 2, false, C>(sm, tw, pc);
+    {   // bottom pass (bits 0..4) with the four-step twiddle, straight to HBM
+        using G = Geom<M, NP - 1>;
+        static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
+        uint32_t* __restrict__ dst = args.work + ((uint64_t)blockIdx.y << args.k);
+        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+            const int col = w & (C - 1);
+            const uint32_t u = w / C;
+            const uint32_t* s = sm + (33 * u) * C + col;
+            uint32_t x[1][32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
+            regs_pass<SET, M, NP - 1, false, 1>(x, u, tw, pc);
+            // slot 32u + q holds k1 = brev5(q) << (M-5) | brev(u): the twiddle
+            // w^(i2*k1) is t * g^brev5(q) with t = w^(i2*brev(u)), g = w^(i2 << (M-5))
+            const uint32_t i2 = c0 + col;
+            uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), args.k);
+            const uint32_t g = fourstep_twiddle<SET>(args.f, prime, i2 << (M - 5), args.k);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int q = brev5(j);
+                x[0][q] = Ar<SET>::mul(x[0][q], t, pc);
+                if (j < 31) t = Ar<SET>::mul(t, g, pc);
+            }
+#pragma unroll
+            for (int q = 0; q < 32; ++q) dst[(uint64_t)(32 * u + q) * N2 + i2] = x[0][q];
+        }
+    }
+}
+
+template <int SET, int M, int C>
+__global__ void __launch_bounds__(256) k_inv_cols(ProdArgs args) {
+    extern __shared__ uint32_t sm[];
+    constexpr int NP = sch_np(M);
+    static_assert(NP >= 2, "column transforms have at least two passes");
+    const int prime = blockIdx.y;
+    const PrimeC pc = args.f.pc[prime];
+    const uint2* __restrict__ tw = args.f.ti[prime];
+    const uint32_t N2 = 1u << args.k2;
+    const uint32_t c0 = blockIdx.x * C;
+    uint32_t* __restrict__ wk = args.work + ((uint64_t)(prime * 2) << args.k);
+    {   // bottom DIT pass (bits 0..4 of the slot) straight from HBM
+        using G = Geom<M, NP - 1>;
+        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+            const int col = w & (C - 1);
+            const uint32_t u = w / C;
+            uint32_t x[1][32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) x[0][q] = wk[(uint64_t)(32 * u + q) * N2 + c0 + col];
+            regs_pass<SET, M, NP - 1, true, 1>(x, u, tw, pc);
+            uint32_t* s = sm + (33 * u) * C + col;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) s[q * C] = x[0][q];
+        }
+        __syncthreads();
+    }
+    col_passes<SET, M, NP - 2, 1, true, C>(sm, tw, pc);
+    {   // top DIT pass: natural row order i1, straight to HBM
+        using G = Geom<M, 0>;
+        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+            const int col = w & (C - 1);
+            const uint32_t u = w / C;
+            const uint32_t* s = sm + G::pbase(u) * C + col;
+            uint32_t x[1][G::R];
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS * C];
+            regs_pass<SET, M, 0, true, 1>(x, u, tw, pc);
+            const uint32_t base = G::base(u);
+#pragma unroll
+            for (int q = 0; q < G::R; ++q)
+                wk[(uint64_t)(base + ((uint32_t)q << G::LO)) * N2 + c0 + col] = x[0][q];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+
+static int col_group(int set, int m) { return (set == 1 && m == 13) ? 4 : kColGroup; }
+
+static size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
+
+#define PREC_COLS_SET0(X) X(0, 6, 8) X(0, 7, 8) X(0, 8, 8) X(0, 9, 8) X(0, 10, 8) X(0, 11, 8)
+#define PREC_COLS_SET1(X) X(1, 12, 8) X(1, 13, 4)
+
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st) {
+    const int m = a.k1, cg = col_group(set, m);
+    const dim3 grid((1u << a.k2) / cg, 2 * kPrimes);
+    const size_t smem = col_smem(m, cg);
+#define X(S, MM, CC) \
+    if (set == S && m == MM) { k_fwd_cols<S, MM, CC><<<grid, 256, smem, st>>>(a); return; }
+    PREC_COLS_SET0(X) PREC_COLS_SET1(X)
+#undef X
+}
+
+void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st) {
+    const int m = a.k1, cg = col_group(set, m);
+    const dim3 grid((1u << a.k2) / cg, kPrimes);
+    const size_t smem = col_smem(m, cg);
+#define X(S, MM, CC) \
+    if (set == S && m == MM) { k_inv_cols<S, MM, CC><<<grid, 256, smem, st>>>(a); return; }
+    PREC_COLS_SET0(X) PREC_COLS_SET1(X)
+#undef X
+}
+
+int configure_cols() {
+    cudaError_t e = cudaSuccess;
+#define X(S, MM, CC)                                                                                    \
+    if (!e) e = cudaFuncSetAttribute(k_fwd_cols<S, MM, CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)col_smem(MM, CC));                                            \
+    if (!e) e = cudaFuncSetAttribute(k_inv_cols<S, MM, CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)col_smem(MM, CC));
+    PREC_COLS_SET0(X) PREC_COLS_SET1(X)
+#undef X
+    return (int)e;
+}
+
+}  // namespace precgpu

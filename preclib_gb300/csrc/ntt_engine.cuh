@@ -1,0 +1,302 @@
+// ntt_engine.cuh -- device-side transform engine shared by the NTT kernels.
+//
+// A sub-transform of 2^M points lives in shared memory with one spare word
+// per 32 (padded index P(i) = i + i/32) and is processed in register passes
+// of radix 2^RB over index bits [LO, LO+RB).  The pass schedule is fixed at
+// compile time: the lowest pass always covers bits 0..4 (RB = 5), every
+// other pass starts at bit 5 or above.  With that schedule the 32 lanes of
+// a warp touch 32 distinct banks in every pass, and every shared-memory
+// address is a per-thread base plus an immediate offset.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ntt_field.cuh"
+#include "ntt_kernels.cuh"
+
+namespace precgpu {
+
+typedef unsigned __int128 u128;
+
+// ---------------------------------------------------------------------------
+// compile-time pass schedule (t = 0 is the top pass, t = np-1 the bottom)
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int sch_np(int m) { return m <= 5 ? 1 : 1 + (m - 5 + 3) / 4; }
+__host__ __device__ constexpr int sch_rb(int m, int t) {
+    return m <= 5 ? m
+                  : (t == sch_np(m) - 1 ? 5
+                                        : (m - 5) / (sch_np(m) - 1) + (t < (m - 5) % (sch_np(m) - 1) ? 1 : 0));
+}
+__host__ __device__ constexpr int sch_lo(int m, int t) { return t < 0 ? m : sch_lo(m, t - 1) - sch_rb(m, t); }
+
+__host__ __device__ constexpr int padded(int n) { return n + (n >> 5); }
+
+// words per array in shared memory (== 4 mod 8)
+__host__ __device__ constexpr int astride_for(int m) { return ((padded(1 << m) + 7) & ~7) + 4; }
+
+template <int M, int T>
+struct Geom {
+    static constexpr int RB = sch_rb(M, T);
+    static constexpr int LO = sch_lo(M, T);
+    static constexpr int R = 1 << RB;
+    static constexpr int LGI = M - RB;  // log2 of items per array
+    static constexpr uint32_t LOMASK = (1u << LO) - 1;
+    // padded distance between consecutive elements of one item
+    static constexpr uint32_t QS = LO >= 5 ? (1u << LO) + (1u << (LO - 5)) : 1u;
+    static __device__ __forceinline__ uint32_t base(uint32_t u) {
+        return ((u >> LO) << (LO + RB)) | (u & LOMASK);
+    }
+    static __device__ __forceinline__ uint32_t pbase(uint32_t u) {
+        const uint32_t b = base(u);
+        return b + (b >> 5);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// register passes
+// ---------------------------------------------------------------------------
+
+// DIF stages over bits LO+RB-1 .. LO of NA arrays held in registers;
+// element q of an item sits at index base + (q << LO); ulo = base & LOMASK.
+template <int SET, int LO, int RB, int NA>
+__device__ __forceinline__ void dif_regs(uint32_t (&x)[NA][1 << RB], uint32_t ulo, const uint2* __restrict__ tw,
+                                         const PrimeC& c) {
+#pragma unroll
+    for (int bb = RB - 1; bb >= 0; --bb) {
+        const int h = 1 << bb;
+#pragma unroll
+        for (int q = 0; q < (1 << RB); ++q) {
+            if (q & h) continue;
+            if (LO == 0 && (q & (h - 1)) == 0) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) Ar<SET>::dif1(x[a][q], x[a][q + h], c);
+                continue;
+            }
+            const uint32_t j = (LO == 0 ? 0u : ulo) | ((uint32_t)(q & (h - 1)) << LO);
+            const uint2 w = __ldg(&tw[(1u << (LO + bb)) + j]);
+#pragma unroll
+            for (int a = 0; a < NA; ++a) Ar<SET>::dif(x[a][q], x[a][q + h], w, c);
+        }
+    }
+}
+
+// DIT stages over bits LO .. LO+RB-1.
+template <int SET, int LO, int RB, int NA>
+__device__ __forceinline__ void dit_regs(uint32_t (&x)[NA][1 << RB], uint32_t ulo, const uint2* __restrict__ tw,
+                                         const PrimeC& c) {
+#pragma unroll
+    for (int bb = 0; bb < RB; ++bb) {
+        const int h = 1 << bb;
+#pragma unroll
+        for (int q = 0; q < (1 << RB); ++q) {
+            if (q & h) continue;
+            if (LO == 0 && (q & (h - 1)) == 0) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) Ar<SET>::dit1(x[a][q], x[a][q + h], c);
+                continue;
+            }
+            const uint32_t j = (LO == 0 ? 0u : ulo) | ((uint32_t)(q & (h - 1)) << LO);
+            const uint2 w = __ldg(&tw[(1u << (LO + bb)) + j]);
+#pragma unroll
+            for (int a = 0; a < NA; ++a) Ar<SET>::dit(x[a][q], x[a][q + h], w, c);
+        }
+    }
+}
+
+template <int SET, int M, int T, bool DIT, int NA>
+__device__ __forceinline__ void regs_pass(uint32_t (&x)[NA][Geom<M, T>::R], uint32_t u, const uint2* __restrict__ tw,
+                                          const PrimeC& c) {
+    using G = Geom<M, T>;
+    if constexpr (DIT) dit_regs<SET, G::LO, G::RB, NA>(x, u & G::LOMASK, tw, c);
+    else dif_regs<SET, G::LO, G::RB, NA>(x, u & G::LOMASK, tw, c);
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory passes
+// ---------------------------------------------------------------------------
+
+// Row layout: array a at sm + a*astride, element i at P(i).  Items of NA
+// arrays share twiddle loads.  narr must be a multiple of NA.
+template <int SET, int M, int T, bool DIT, int NA>
+__device__ __forceinline__ void row_pass(uint32_t* sm, int astride, int narr, const uint2* __restrict__ tw,
+                                         const PrimeC& c) {
+    using G = Geom<M, T>;
+    const int total = (narr / NA) << G::LGI;
+    for (int w = threadIdx.x; w < total; w += blockDim.x) {
+        const uint32_t u = w & ((1u << G::LGI) - 1);
+        const int g = w >> G::LGI;
+        uint32_t* s = sm + g * NA * astride + G::pbase(u);
+        uint32_t x[NA][G::R];
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) x[a][q] = s[a * astride + q * G::QS];
+        regs_pass<SET, M, T, DIT, NA>(x, u, tw, c);
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) s[a * astride + q * G::QS] = x[a][q];
+    }
+}
+
+// Column layout: C interleaved columns, element i of column c at
+// P(i)*C + c; lanes cover C adjacent columns (twiddle loads broadcast).
+template <int SET, int M, int T, bool DIT, int C>
+__device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
+    using G = Geom<M, T>;
+    const int total = C << G::LGI;
+    for (int w = threadIdx.x; w < total; w += blockDim.x) {
+        const int col = w & (C - 1);
+        const uint32_t u = w / C;
+        uint32_t* s = sm + G::pbase(u) * C + col;
+        uint32_t x[1][G::R];
+#pragma unroll
+        for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS * C];
+        regs_pass<SET, M, T, DIT, 1>(x, u, tw, c);
+#pragma unroll
+        for (int q = 0; q < G::R; ++q) s[q * G::QS * C] = x[0][q];
+    }
+}
+
+// Middle passes T in [T0, T1] (ascending for DIF, descending for DIT).
+template <int SET, int M, int T, int TEND, bool DIT, int NA>
+__device__ __forceinline__ void row_passes(uint32_t* sm, int astride, int narr, const uint2* __restrict__ tw,
+                                           const PrimeC& c) {
+    if constexpr (DIT ? (T >= TEND) : (T <= TEND)) {
+        row_pass<SET, M, T, DIT, NA>(sm, astride, narr, tw, c);
+        __syncthreads();
+        row_passes<SET, M, DIT ? T - 1 : T + 1, TEND, DIT, NA>(sm, astride, narr, tw, c);
+    }
+}
+
+template <int SET, int M, int T, int TEND, bool DIT, int C>
+__device__ __forceinline__ void col_passes(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
+    if constexpr (DIT ? (T >= TEND) : (T <= TEND)) {
+        col_pass<SET, M, T, DIT, C>(sm, tw, c);
+        __syncthreads();
+        col_passes<SET, M, DIT ? T - 1 : T + 1, TEND, DIT, C>(sm, tw, c);
+    }
+}
+
+// bit reversal of the low `bits` bits
+__device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) { return bits ? __brev(x) >> (32 - bits) : 0u; }
+
+__host__ __device__ constexpr int brev5(int q) {
+    return ((q & 1) << 4) | ((q & 2) << 2) | (q & 4) | ((q & 8) >> 2) | ((q & 16) >> 4);
+}
+
+// w^e * 2^32 mod p (Montgomery form, [0, 2p)) for a root w of order
+// N = 2^k, e < N; two-level table over the set's largest root.
+template <int SET>
+__device__ __forceinline__ uint32_t fourstep_twiddle(const FieldArgs& f, int prime, uint32_t e, int k) {
+    const uint32_t E = e << (f.max_log2 - k);
+    const uint32_t hi = __ldg(&f.twhi[prime][E >> kTwLevelBits]);
+    const uint32_t lo = __ldg(&f.twlo[prime][E & ((1u << kTwLevelBits) - 1)]);
+    return Ar<SET>::mul(hi, lo, f.pc[prime]);
+}
+
+// ---------------------------------------------------------------------------
+// CRT and carries
+// ---------------------------------------------------------------------------
+
+// Garner recombination of the three inverse-transform outputs (any value
+// below 2^32 of each residue class) into the exact coefficient below
+// p1*p2*p3, with the transform scale folded into the constants
+// (src/mul_ntt.cpp:405-424 recombines its primes the same way).
+__device__ __forceinline__ u128 crt3(uint32_t y1, uint32_t y2, uint32_t y3, const CrtConst& cc, const FieldArgs& f) {
+    const uint32_t p1 = f.pc[0].p, p2 = f.pc[1].p, p3 = f.pc[2].p;
+    const uint32_t v1 = shoup_mul(y1, cc.s1, p1);
+    const uint32_t v2 = sub_mod(shoup_mul(y2, cc.k22, p2), shoup_mul(v1, cc.k21, p2), p2);
+    uint32_t v3 = sub_mod(shoup_mul(y3, cc.k33, p3), shoup_mul(v1, cc.k31, p3), p3);
+    v3 = sub_mod(v3, shoup_mul(v2, cc.k32, p3), p3);
+    const uint64_t t = (uint64_t)v2 + (uint64_t)p2 * v3;
+    return (u128)t * p1 + v1;
+}
+
+// Carry-in of every lane from the lanes' (G, P) bits: the chain
+// c_{t+1} = G_t | (P_t & c_t) is the carry chain of the sum A + B with
+// A = G|P, B = G (G and P are disjoint), so the carry into lane t is bit t
+// of (A + B + cin) ^ A ^ B.
+__device__ __forceinline__ uint64_t carry_chain(uint32_t G, uint32_t P, bool cin) {
+    const uint64_t A = (uint64_t)(G | P), B = (uint64_t)G;
+    return (A + B + (cin ? 1u : 0u)) ^ A ^ B;  // bit t: carry into t; bit 32: carry out
+}
+
+struct BlockCarryShared {
+    uint32_t wg[32], wp[32];
+    uint32_t block_cin;
+};
+
+// Block-wide carry resolution: every thread holds (G, P) of its limbs; the
+// block aggregate (Gb, Pb) goes to cin_fn (thread 0 only), which returns
+// the block's carry-in; returns the thread's carry-in.
+template <class CinFn>
+__device__ __forceinline__ bool block_carry(bool G, bool P, BlockCarryShared& sh, CinFn cin_fn) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    const uint32_t gm = __ballot_sync(0xffffffffu, G);
+    const uint32_t pm = __ballot_sync(0xffffffffu, P);
+    if (lane == 0) {
+        sh.wg[warp] = (uint32_t)(carry_chain(gm, pm, false) >> 32) & 1;
+        sh.wp[warp] = pm == 0xffffffffu;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const bool wG = lane < nwarps ? sh.wg[lane] != 0 : false;
+        const bool wP = lane < nwarps ? sh.wp[lane] != 0 : true;
+        const uint32_t real = nwarps >= 32 ? 0xffffffffu : ((1u << nwarps) - 1);
+        const uint32_t bg = __ballot_sync(0xffffffffu, wG) & real;
+        const uint32_t bp = __ballot_sync(0xffffffffu, wP) & real;
+        const uint64_t c0 = carry_chain(bg, bp, false);
+        const bool Gb = (c0 >> nwarps) & 1;
+        const bool Pb = bp == real;
+        uint32_t bcin = 0;
+        if (lane == 0) bcin = cin_fn(Gb, Pb) ? 1u : 0u;
+        bcin = __shfl_sync(0xffffffffu, bcin, 0);
+        const uint64_t cw = carry_chain(bg, bp, bcin != 0);
+        __syncwarp();
+        if (lane < nwarps) sh.wg[lane] = (uint32_t)(cw >> lane) & 1;  // carry into warp `lane`
+    }
+    __syncthreads();
+    const bool wcin = sh.wg[warp] != 0;
+    const uint64_t cl = carry_chain(gm, pm, wcin);
+    return (cl >> lane) & 1;
+}
+
+// Limbs of one thread: T_k = c_{2k} + c_{2k+1} * 2^32 folds the 32-bit
+// digit convolution onto 64-bit limbs (T < 2^123); limb value
+// v_k = lo64(T_k) + hi(T_{k-1}) with generate bit g_k.  Returns (G, P):
+// the carry out with carry-in 0, and whether a carry-in passes through.
+template <int L>
+__device__ __forceinline__ void limbs_from_sums(const u128 (&T)[L], uint64_t prev_hi, uint64_t (&v)[L],
+                                                uint32_t& gbits, bool& G, bool& P) {
+    gbits = 0;
+    bool c = false;
+    P = true;
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        const uint64_t hi_prev = k == 0 ? prev_hi : (uint64_t)(T[k - 1] >> 64);
+        const u128 s = (u128)(uint64_t)T[k] + hi_prev;
+        v[k] = (uint64_t)s;
+        const bool g = (uint64_t)(s >> 64) != 0;
+        gbits |= (uint32_t)g << k;
+        const bool all1 = v[k] == ~0ull;
+        c = g || (all1 && c);
+        P = P && all1;
+    }
+    G = c;
+}
+
+template <int L>
+__device__ __forceinline__ void limbs_finish(int64_t m0, uint64_t lout, const uint64_t (&v)[L], uint32_t gbits,
+                                             bool cin, uint64_t* out) {
+    bool c = cin;
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+        const uint64_t r = v[k] + (c ? 1u : 0u);
+        const bool g = (gbits >> k) & 1;
+        c = g || (v[k] == ~0ull && c);
+        if (m0 + k < (int64_t)lout) out[m0 + k] = r;
+    }
+}
+
+}  // namespace precgpu

@@ -1,4 +1,4 @@
-// ntt_kernels.cuh -- shared declarations between the NTT kernels and the host.
+// ntt_kernels.cuh -- declarations shared by the NTT kernels and the host.
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -9,18 +9,22 @@
 
 namespace precgpu {
 
-// CRT constants of one transform length (Garner with the transform's
-// scaling folded in; see crt3 in ntt_kernels.cu).
-struct CrtConst {
-    ShoupC s1, k21, k22, k31, k32, k33;
+// Constants and device tables of one prime set, passed to every kernel by
+// value (kernel parameter space).
+struct FieldArgs {
+    PrimeC pc[kPrimes];
+    const uint2* tf[kPrimes];      // tf[(1<<b)+j] = (w_{2^{b+1}}^j, Shoup), b < 13
+    const uint2* ti[kPrimes];      // ti[(1<<b)+j] = (w_{2^{b+1}}^-j, Shoup)
+    const uint32_t* twhi[kPrimes]; // w_{2^L}^(h*2^13) * 2^32 mod p, L = set cap
+    const uint32_t* twlo[kPrimes]; // w_{2^L}^l * 2^32 mod p, l < 2^13
+    int max_log2;                  // L
+    int pad;
 };
 
-// Device tables of the three primes (set once per device).
-struct TableSet {
-    const uint2* tf[kPrimes];      // tf[(1<<b)+j] = (w_{2^{b+1}}^j, Shoup), b < 13
-    const uint2* ti[kPrimes];      // ti[(1<<b)+j] = (w_{2^{b+1}}^{-j}, Shoup)
-    const uint32_t* twhi[kPrimes]; // w_{2^26}^{h*2^13} * 2^32 mod p, h < 2^13
-    const uint32_t* twlo[kPrimes]; // w_{2^26}^{l} * 2^32 mod p, l < 2^13
+// CRT constants of one transform length (Garner with the transform's
+// scale 2^32 * N^-1 folded in; see crt3 in ntt_engine.cuh).
+struct CrtConst {
+    ShoupC s1, k21, k22, k31, k32, k33;
 };
 
 // One product of the multi-pass (four-step) path.
@@ -30,15 +34,18 @@ struct ProdArgs {
     uint64_t* out;
     uint32_t* work;     // [prime][operand][N] residues
     uint32_t* scratch;  // carry look-back: [0] block ticket, [1..nblk] status words
-    int* err;           // error bits (PREC_GPU_DEVERR_*)
+    int* err;           // error bits (kDevErr*)
     uint64_t la, lb, lout;
     int k, k1, k2;      // log2 of N, of the column length N1, of the row length N2
     int nblk;           // blocks of the carry kernel
+    int rows;           // rows per CTA of the row pass
+    int pad;
     CrtConst crt;
+    FieldArgs f;
 };
 
-// One product of the single-CTA path (small transforms, also the batch
-// form's small length classes).
+// One product of the single-CTA path (transforms up to 2^12 points; also
+// the batch form's small length classes).  Always prime set 0.
 struct SmallDesc {
     const uint64_t* a;
     const uint64_t* b;
@@ -53,14 +60,29 @@ struct SmallDesc {
 constexpr int kDevErrTimeout = 1;
 constexpr int kDevErrCarry = 2;
 
-// host-side launchers (ntt_kernels.cu)
-void ntt_set_tables(const PrimeC* primes, const TableSet& tabs);
-int ntt_small_max_log2();
+constexpr int kSmallMaxLog2 = 12;
+constexpr int kSmallMinLog2 = 5;
+constexpr int kCarryThreads = 256;
+constexpr int kCarryLimbs = 4;  // limbs per thread in the carry kernel
+constexpr int kColGroup = 8;    // adjacent columns per column-pass CTA (4 when N1 = 2^13)
+
+// host-side launchers; `ev` (optional) gets an event recorded before the
+// first kernel and after each kernel.
 size_t ntt_small_smem_bytes(int k);
-// d_descs: device array of `count` products, or null with `single` (by value)
-void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k, cudaStream_t st);
-void ntt_launch_4step(const ProdArgs& args, cudaStream_t st);
-int ntt_carry_block_limbs();
-int ntt_configure_kernels();  // opt-in shared memory sizes; returns cudaError_t
+int ntt_small_threads(int k);
+void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k,
+                      const FieldArgs& f, cudaStream_t st, cudaEvent_t* ev = nullptr);
+void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev = nullptr);
+int ntt_row_threads(int k2, int n1, int* rows);
+int ntt_configure_kernels();  // opt-in shared-memory sizes; returns a cudaError_t
+
+// launchers of each translation unit (ntt_cols.cu, ntt_rows.cu, ntt_carry.cu, ntt_small.cu)
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st);
+void launch_rows(int set, const ProdArgs& a, cudaStream_t st);
+void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st);
+void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st);
+int configure_cols();
+int configure_rows();
+int configure_small();
 
 }  // namespace precgpu

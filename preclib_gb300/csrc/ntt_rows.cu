@@ -1,0 +1,143 @@
+// ntt_rows.cu -- row pass of the four-step NTT.
+//
+// For `rows` row slots s of one prime: the remaining DIF stages of both
+// operands' rows (the last log2(N2) stages of ntt_forward,
+// src/mul_ntt.cpp:193-255), the pointwise product (mul_ntt.cpp:364-373),
+// the first DIT stages of the product row (ntt_inverse, mul_ntt.cpp:257-311)
+// and the inverse four-step twiddle w_N^-(i2*k1), k1 = bitrev(s).  The
+// bottom five stages of both directions and the product run in registers
+// without a shared-memory round trip in between.
+#include "ntt_engine.cuh"
+
+namespace precgpu {
+
+template <int SET, int M>
+__global__ void __launch_bounds__(256) k_rows(ProdArgs args) {
+    extern __shared__ uint32_t sm[];
+    constexpr int NP = sch_np(M);
+    static_assert(NP >= 2, "row transforms have at least two passes");
+    constexpr int AS = astride_for(M);
+    const int prime = blockIdx.y;
+    const PrimeC pc = args.f.pc[prime];
+    const uint2* __restrict__ twf = args.f.tf[prime];
+    const uint2* __restrict__ twi = args.f.ti[prime];
+    const int rows = args.rows;
+    uint32_t* __restrict__ A = args.work + ((uint64_t)(prime * 2) << args.k);
+    const uint32_t* __restrict__ B = A + (1ull << args.k);
+    const uint32_t row0 = blockIdx.x * rows;
+
+    {   // top DIF pass of A and B straight from HBM (shared twiddles)
+        using G = Geom<M, 0>;
+        for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
+            const int r = w >> G::LGI;
+            const uint32_t u = w & ((1u << G::LGI) - 1);
+            const uint64_t roff = ((uint64_t)(row0 + r) << M) + G::base(u);
+            uint32_t x[2][G::R];
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) {
+                x[0][q] = A[roff + ((uint32_t)q << G::LO)];
+                x[1][q] = B[roff + ((uint32_t)q << G::LO)];
+            }
+            regs_pass<SET, M, 0, false, 2>(x, u, twf, pc);
+            uint32_t* s = sm + 2 * r * AS + G::pbase(u);
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) {
+                s[q * G::QS] = x[0][q];
+                s[AS + q * G::QS] = x[1][q];
+            }
+        }
+        __syncthreads();
+    }
+    row_passes<SET, M, 1, NP - 2, false, 2>(sm, AS, 2 * rows, twf, pc);
+    {   // bottom: last DIF stages of A and B, product, first DIT stages
+        using G = Geom<M, NP - 1>;
+        static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
+        for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
+            const int r = w >> G::LGI;
+            const uint32_t u = w & ((1u << G::LGI) - 1);
+            uint32_t* s = sm + 2 * r * AS + 33 * u;
+            uint32_t x[2][32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                x[0][q] = s[q];
+                x[1][q] = s[AS + q];
+            }
+            regs_pass<SET, M, NP - 1, false, 2>(x, u, twf, pc);
+            uint32_t y[1][32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) y[0][q] = Ar<SET>::mul(x[0][q], x[1][q], pc);
+            regs_pass<SET, M, NP - 1, true, 1>(y, u, twi, pc);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) s[q] = y[0][q];
+        }
+        __syncthreads();
+    }
+    row_passes<SET, M, NP - 2, 1, true, 1>(sm, 2 * AS, rows, twi, pc);
+    {   // top DIT pass with the inverse four-step twiddle, straight to HBM
+        using G = Geom<M, 0>;
+        const uint32_t nmask = (uint32_t)((1ull << args.k) - 1);
+        for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
+            const int r = w >> G::LGI;
+            const uint32_t u = w & ((1u << G::LGI) - 1);
+            const uint32_t* s = sm + 2 * r * AS + G::pbase(u);
+            uint32_t x[1][G::R];
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS];
+            regs_pass<SET, M, 0, true, 1>(x, u, twi, pc);
+            // element q is i2 = base + (q << LO); twiddle w^-(i2*k1) = t * g^q
+            const uint32_t srow = row0 + r;
+            const uint32_t k1v = brev_bits(srow, args.k1);
+            const uint32_t base = G::base(u);
+            uint32_t t = fourstep_twiddle<SET>(args.f, prime, (0u - base * k1v) & nmask, args.k);
+            const uint32_t g = fourstep_twiddle<SET>(args.f, prime, (0u - (k1v << G::LO)) & nmask, args.k);
+            uint32_t* __restrict__ dst = A + ((uint64_t)srow << M) + base;
+#pragma unroll
+            for (int q = 0; q < G::R; ++q) {
+                dst[(uint32_t)q << G::LO] = Ar<SET>::mul(Ar<SET>::half(x[0][q], pc), t, pc);
+                if (q < G::R - 1) t = Ar<SET>::mul(t, g, pc);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+
+static size_t row_smem(int m, int rows) { return (size_t)rows * 2 * astride_for(m) * sizeof(uint32_t); }
+
+// rows per CTA: one 256-thread CTA covers 256 / 2^(M-5) rows, fewer when
+// the transform has too few rows to fill the GPU, never under one warp
+int ntt_row_threads(int k2, int n1, int* rows_out) {
+    int rows = 256 >> (k2 - 5);
+    if (rows < 1) rows = 1;
+    while (rows > 1 && (n1 / rows) * kPrimes < 2 * 152) rows >>= 1;
+    int min_rows = k2 >= 10 ? 1 : (1 << (10 - k2));  // >= 32 threads
+    if (rows < min_rows) rows = min_rows;
+    if (rows > n1) rows = n1;
+    *rows_out = rows;
+    return rows << (k2 - 5);
+}
+
+#define PREC_ROWS(X) X(0, 7) X(0, 8) X(0, 9) X(0, 10) X(0, 11) X(0, 12) X(1, 12) X(1, 13)
+
+void launch_rows(int set, const ProdArgs& a, cudaStream_t st) {
+    const int m = a.k2;
+    const dim3 grid((1u << a.k1) / a.rows, kPrimes);
+    const int threads = a.rows << (m - 5);
+    const size_t smem = row_smem(m, a.rows);
+#define X(S, MM) \
+    if (set == S && m == MM) { k_rows<S, MM><<<grid, threads, smem, st>>>(a); return; }
+    PREC_ROWS(X)
+#undef X
+}
+
+int configure_rows() {
+    cudaError_t e = cudaSuccess;
+#define X(S, MM)                                                                                   \
+    if (!e) e = cudaFuncSetAttribute(k_rows<S, MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)row_smem(MM, 256 >> (MM - 5) > 0 ? 256 >> (MM - 5) : 1));
+    PREC_ROWS(X)
+#undef X
+    return (int)e;
+}
+
+}  // namespace precgpu

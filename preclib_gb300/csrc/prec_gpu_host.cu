@@ -23,9 +23,12 @@ namespace precgpu {
 
 typedef unsigned __int128 u128;
 
-// The reference's NTT primes and generators (src/mul_ntt.cpp:29-34).
-static const uint32_t kP[kPrimes] = {469762049u, 1811939329u, 2013265921u};
-static const uint32_t kG[kPrimes] = {3u, 13u, 31u};
+// Prime sets (see ntt_field.cuh): set 0 for transforms up to 2^23 points,
+// set 1 -- the reference's primes and generators, src/mul_ntt.cpp:29-34 --
+// for 2^24 .. 2^26 points.
+static const uint32_t kP[kSets][kPrimes] = {{998244353u, 897581057u, 880803841u},
+                                            {469762049u, 1811939329u, 2013265921u}};
+static const uint32_t kG[kSets][kPrimes] = {{3u, 3u, 26u}, {3u, 13u, 31u}};
 
 static uint32_t powmod(uint64_t b, uint64_t e, uint32_t m) {
     uint64_t r = 1 % m;
@@ -55,21 +58,34 @@ static uint32_t neg_inv32(uint32_t m) {  // -m^{-1} mod 2^32 (Newton on 2-adic i
     return 0u - x;
 }
 
+constexpr int kMaxStages = 8;
+
+// kernel names of each path, in launch order
+static const char* const kStageNames[3][kMaxStages] = {
+    {"k_small"},
+    {"k_fwd_cols", "k_rows", "k_inv_cols", "k_crt_carry"},
+    {"k_fft"},
+};
+static const int kStageCount[3] = {1, 4, 1};
+
 struct Plan {
     int k = 0, k1 = 0, k2 = 0;
+    int set = 0;
     int path = 0;  // 0 single CTA, 1 four-step
     int nblk = 0;
+    int rows = 0;  // rows per CTA of the row pass
     CrtConst crt{};
     size_t work_bytes = 0;
 };
 
-static CrtConst crt_for(int k) {
-    const uint32_t p1 = kP[0], p2 = kP[1], p3 = kP[2];
+static CrtConst crt_for(int set, int k) {
+    const uint32_t* P = kP[set];
+    const uint32_t p1 = P[0], p2 = P[1], p3 = P[2];
     uint32_t s[kPrimes];
     for (int j = 0; j < kPrimes; ++j) {
-        const uint32_t R = (uint32_t)((1ull << 32) % kP[j]);
-        const uint32_t ninv = invmod((uint32_t)((1ull << k) % kP[j]), kP[j]);
-        s[j] = mulmod(R, ninv, kP[j]);
+        const uint32_t R = (uint32_t)((1ull << 32) % P[j]);
+        const uint32_t ninv = invmod((uint32_t)((1ull << k) % P[j]), P[j]);
+        s[j] = mulmod(R, ninv, P[j]);
     }
     const uint32_t c12 = invmod(p1 % p2, p2), c13 = invmod(p1 % p3, p3), c23 = invmod(p2 % p3, p3);
     CrtConst c;
@@ -86,12 +102,13 @@ static CrtConst crt_for(int k) {
 // da, db: 32-bit digit counts (upper bounds are fine)
 static int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
     const uint64_t need = da + db - 1;
-    int k = 5;
+    int k = kSmallMinLog2;
     while ((1ull << k) < need) ++k;
-    if (k > kMaxLog2N) return PREC_GPU_E_TOO_LARGE;
+    if (k > kSetMaxLog2[kSets - 1]) return PREC_GPU_E_TOO_LARGE;
     pl.k = k;
-    pl.crt = crt_for(k);
-    if (k <= ntt_small_max_log2()) {
+    pl.set = k <= kSetMaxLog2[0] ? 0 : 1;
+    pl.crt = crt_for(pl.set, k);
+    if (k <= kSmallMaxLog2) {
         pl.path = 0;
         pl.work_bytes = 0;
         return 0;
@@ -99,7 +116,8 @@ static int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
     pl.path = 1;
     pl.k1 = k / 2;
     pl.k2 = k - pl.k1;
-    const uint64_t bl = (uint64_t)ntt_carry_block_limbs();
+    ntt_row_threads(pl.k2, 1 << pl.k1, &pl.rows);
+    const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
     pl.nblk = (int)((lout + bl - 1) / bl);
     pl.work_bytes = ((size_t)2 * kPrimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
     return 0;
@@ -118,6 +136,8 @@ struct Ctx {
     int* d_err = nullptr;
     int* h_err = nullptr;
     cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t stage_ev[kMaxStages + 1] = {};
+    FieldArgs field[kSets] = {};
 };
 
 static Ctx g_ctx;
@@ -136,60 +156,67 @@ static int cuda_code(cudaError_t e) {
         if (_e != cudaSuccess) return cuda_code(_e); \
     } while (0)
 
+// Per set and prime: Shoup tables of the sub-transform roots (forward and
+// inverse, b < 13) and the two-level four-step table of the set's largest
+// root in Montgomery form.
 static int build_tables(Ctx& c) {
     const int T = 1 << kMaxSubLog2;   // entries of the Shoup tables
     const int H = 1 << kTwLevelBits;  // entries of each four-step level
     const size_t per_prime = (size_t)2 * T * sizeof(uint2) + (size_t)2 * H * sizeof(uint32_t);
-    std::vector<uint8_t> host(per_prime * kPrimes);
-    PrimeC primes[kPrimes];
-    TableSet tabs;
+    std::vector<uint8_t> host(per_prime * kPrimes * kSets);
     CK(cudaMalloc(&c.tables, host.size()));
-    for (int j = 0; j < kPrimes; ++j) {
-        const uint32_t p = kP[j];
-        primes[j].p = p;
-        primes[j].pinv = neg_inv32(p);
-        primes[j].one_wp = (uint32_t)((1ull << 32) / p);
-        primes[j].pad = 0;
-        // generator check: g^((p-1)/2) == -1, so w26 has order exactly 2^26
-        if (powmod(kG[j], (p - 1) / 2, p) != p - 1) return PREC_GPU_E_INTERNAL;
-        const uint32_t w26 = powmod(kG[j], (p - 1) >> kMaxLog2N, p);
-        uint8_t* base = host.data() + per_prime * j;
-        uint2* tf = reinterpret_cast<uint2*>(base);
-        uint2* ti = tf + T;
-        uint32_t* twhi = reinterpret_cast<uint32_t*>(ti + T);
-        uint32_t* twlo = twhi + H;
-        tf[0] = make_uint2(1, (uint32_t)((1ull << 32) / p));
-        ti[0] = tf[0];
-        for (int b = 0; b < kMaxSubLog2; ++b) {
-            const uint32_t wb = powmod(w26, 1ull << (kMaxLog2N - b - 1), p);  // order 2^(b+1)
-            const uint32_t wbi = invmod(wb, p);
-            uint32_t x = 1, y = 1;
-            for (int i = 0; i < (1 << b); ++i) {
-                const ShoupC f = shoup(x, p), g = shoup(y, p);
-                tf[(1 << b) + i] = make_uint2(f.w, f.wp);
-                ti[(1 << b) + i] = make_uint2(g.w, g.wp);
-                x = mulmod(x, wb, p);
-                y = mulmod(y, wbi, p);
+    for (int set = 0; set < kSets; ++set) {
+        FieldArgs& fa = c.field[set];
+        const int L = kSetMaxLog2[set];
+        fa.max_log2 = L;
+        fa.pad = 0;
+        for (int j = 0; j < kPrimes; ++j) {
+            const uint32_t p = kP[set][j];
+            PrimeC& pc = fa.pc[j];
+            pc.p = p;
+            pc.pinv = neg_inv32(p);
+            pc.one_wp = (uint32_t)((1ull << 32) / p);
+            pc.p2 = 2 * p;
+            // g^((p-1)/2) == -1, so wL = g^((p-1)/2^L) has order exactly 2^L
+            if (powmod(kG[set][j], (p - 1) / 2, p) != p - 1) return PREC_GPU_E_INTERNAL;
+            if (((p - 1) >> L) << L != p - 1) return PREC_GPU_E_INTERNAL;
+            const uint32_t wL = powmod(kG[set][j], (p - 1) >> L, p);
+            const size_t off = per_prime * (set * kPrimes + j);
+            uint2* tf = reinterpret_cast<uint2*>(host.data() + off);
+            uint2* ti = tf + T;
+            uint32_t* twhi = reinterpret_cast<uint32_t*>(ti + T);
+            uint32_t* twlo = twhi + H;
+            tf[0] = make_uint2(1, (uint32_t)((1ull << 32) / p));
+            ti[0] = tf[0];
+            for (int b = 0; b < kMaxSubLog2; ++b) {
+                const uint32_t wb = powmod(wL, 1ull << (L - b - 1), p);  // order 2^(b+1)
+                const uint32_t wbi = invmod(wb, p);
+                uint32_t x = 1, y = 1;
+                for (int i = 0; i < (1 << b); ++i) {
+                    const ShoupC f = shoup(x, p), g = shoup(y, p);
+                    tf[(1 << b) + i] = make_uint2(f.w, f.wp);
+                    ti[(1 << b) + i] = make_uint2(g.w, g.wp);
+                    x = mulmod(x, wb, p);
+                    y = mulmod(y, wbi, p);
+                }
             }
+            const uint32_t R = (uint32_t)((1ull << 32) % p);
+            const uint32_t step_hi = powmod(wL, (uint64_t)H, p);
+            uint32_t x = R, y = R;
+            for (int i = 0; i < H; ++i) {
+                twhi[i] = x;
+                twlo[i] = y;
+                x = mulmod(x, step_hi, p);
+                y = mulmod(y, wL, p);
+            }
+            const uint8_t* dbase = static_cast<uint8_t*>(c.tables) + off;
+            fa.tf[j] = reinterpret_cast<const uint2*>(dbase);
+            fa.ti[j] = fa.tf[j] + T;
+            fa.twhi[j] = reinterpret_cast<const uint32_t*>(fa.ti[j] + T);
+            fa.twlo[j] = fa.twhi[j] + H;
         }
-        const uint32_t R = (uint32_t)((1ull << 32) % p);
-        const uint32_t step_hi = powmod(w26, (uint64_t)H, p);
-        uint32_t x = R, y = R;
-        for (int i = 0; i < H; ++i) {
-            twhi[i] = x;
-            twlo[i] = y;
-            x = mulmod(x, step_hi, p);
-            y = mulmod(y, w26, p);
-        }
-        const uint8_t* dbase = static_cast<uint8_t*>(c.tables) + per_prime * j;
-        tabs.tf[j] = reinterpret_cast<const uint2*>(dbase);
-        tabs.ti[j] = tabs.tf[j] + T;
-        tabs.twhi[j] = reinterpret_cast<const uint32_t*>(tabs.ti[j] + T);
-        tabs.twlo[j] = tabs.twhi[j] + H;
     }
     CK(cudaMemcpy(c.tables, host.data(), host.size(), cudaMemcpyHostToDevice));
-    ntt_set_tables(primes, tabs);
-    CK(cudaGetLastError());
     return 0;
 }
 
@@ -206,6 +233,7 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaEventCreateWithFlags(&c.last_done, cudaEventDisableTiming));
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
+    for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&c.stage_ev[i]));
     CK(cudaMalloc(&c.d_err, sizeof(int)));
     CK(cudaMemset(c.d_err, 0, sizeof(int)));
     CK(cudaMallocHost(&c.h_err, sizeof(int)));
@@ -256,7 +284,7 @@ static int ensure_io(Ctx& c, size_t limbs) {
 
 // Enqueues one NTT-band product on device pointers.
 static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
-                       uint64_t* d_out, const Plan& pl, cudaStream_t st) {
+                       uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     const uint64_t lout = la + lb;
     if (pl.path == 0) {
         SmallDesc d;
@@ -269,7 +297,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         d.k = pl.k;
         d.pad = 0;
         d.crt = pl.crt;
-        ntt_launch_small(nullptr, &d, 1, pl.k, st);
+        ntt_launch_small(nullptr, &d, 1, pl.k, c.field[0], st, ev);
     } else {
         ProdArgs args;
         args.a = d_a;
@@ -285,8 +313,11 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.k1 = pl.k1;
         args.k2 = pl.k2;
         args.nblk = pl.nblk;
+        args.rows = pl.rows;
+        args.pad = 0;
         args.crt = pl.crt;
-        ntt_launch_4step(args, st);
+        args.f = c.field[pl.set];
+        ntt_launch_4step(pl.set, args, st, ev);
     }
     CK(cudaGetLastError());
     return 0;
@@ -371,6 +402,7 @@ void prec_gpu_shutdown(void) {
     cudaEventDestroy(c.last_done);
     cudaEventDestroy(c.ev0);
     cudaEventDestroy(c.ev1);
+    for (int i = 0; i <= kMaxStages; ++i) cudaEventDestroy(c.stage_ev[i]);
     cudaStreamDestroy(c.stream);
     c.ws = nullptr;
     c.io = nullptr;
@@ -402,6 +434,32 @@ int prec_gpu_mul_device(const uint64_t* d_a, size_t an, const uint64_t* d_b, siz
     if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st))) return r;
     CK(cudaEventRecord(c.last_done, st));
     return 0;
+}
+
+int prec_gpu_mul_device_profile(const uint64_t* d_a, size_t an, const uint64_t* d_b, size_t bn,
+                                uint64_t* d_out, void* stream, float* stage_ms, int* nstages) {
+    if (!d_a || !d_b || !d_out || an == 0 || bn == 0 || !stage_ms || !nstages) return PREC_GPU_E_ARG;
+    Ctx& c = g_ctx;
+    std::lock_guard<std::mutex> lk(c.mu);
+    int r = init_locked(c, -1);
+    if (r) return r;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Plan pl;
+    if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl))) return r;
+    if ((r = ensure_ws(c, pl.work_bytes))) return r;
+    CK(cudaStreamWaitEvent(st, c.last_done, 0));
+    if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st, c.stage_ev))) return r;
+    CK(cudaEventRecord(c.last_done, st));
+    CK(cudaStreamSynchronize(st));
+    const int n = kStageCount[pl.path];
+    for (int i = 0; i < n; ++i) CK(cudaEventElapsedTime(&stage_ms[i], c.stage_ev[i], c.stage_ev[i + 1]));
+    *nstages = n;
+    return 0;
+}
+
+const char* prec_gpu_stage_name(int path, int stage) {
+    if (path < 0 || path > 2 || stage < 0 || stage >= kStageCount[path]) return "";
+    return kStageNames[path][stage];
 }
 
 int prec_gpu_stream_check(void* stream) {

@@ -21,7 +21,8 @@ E_ARG, E_TOO_LARGE, E_NOMEM, E_CUDA, E_TIMEOUT, E_FFT_ROUNDING, E_NODEV, E_INTER
 EXPORTS = (
     "prec_gpu_init", "prec_gpu_shutdown", "prec_gpu_mul", "prec_gpu_mul_ntt",
     "prec_gpu_mul_device", "prec_gpu_stream_check", "prec_gpu_last_stats",
-    "prec_gpu_ntt_log2", "prec_gpu_strerror",
+    "prec_gpu_ntt_log2", "prec_gpu_strerror", "prec_gpu_mul_device_profile",
+    "prec_gpu_stage_name",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -66,6 +67,13 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_last_stats.restype = ctypes.c_int
         L.prec_gpu_ntt_log2.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
         L.prec_gpu_ntt_log2.restype = ctypes.c_int
+        L.prec_gpu_mul_device_profile.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                                  ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.POINTER(ctypes.c_float),
+                                                  ctypes.POINTER(ctypes.c_int)]
+        L.prec_gpu_mul_device_profile.restype = ctypes.c_int
+        L.prec_gpu_stage_name.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.prec_gpu_stage_name.restype = ctypes.c_char_p
         L.prec_gpu_strerror.argtypes = [ctypes.c_int]
         L.prec_gpu_strerror.restype = ctypes.c_char_p
         _LIB = L
@@ -109,6 +117,16 @@ def mul_device(a_ptr: int, an: int, b_ptr: int, bn: int, out_ptr: int, stream: i
     """Enqueue a product on device pointers (e.g. torch tensors' data_ptr())."""
     check(lib().prec_gpu_mul_device(a_ptr, an, b_ptr, bn, out_ptr, stream or None),
           "prec_gpu_mul_device")
+
+
+def mul_device_profile(a_ptr: int, an: int, b_ptr: int, bn: int, out_ptr: int, stream: int = 0):
+    """Run one product on device pointers; returns [(kernel name, ms), ...]."""
+    ms = (ctypes.c_float * 8)()
+    n = ctypes.c_int(0)
+    check(lib().prec_gpu_mul_device_profile(a_ptr, an, b_ptr, bn, out_ptr, stream or None, ms,
+                                            ctypes.byref(n)), "prec_gpu_mul_device_profile")
+    path = 0 if n.value == 1 else 1
+    return [(lib().prec_gpu_stage_name(path, i).decode(), float(ms[i])) for i in range(n.value)]
 
 
 def stream_check(stream: int = 0) -> None:

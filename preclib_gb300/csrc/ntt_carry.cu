@@ -1,43 +1,35 @@
 // ntt_carry.cu -- CRT recombination and carry propagation of the four-step
 // path: the reference's ntt_crt2/ntt_crt3 and serial ntt_from_residues
 // carry loop (src/mul_ntt.cpp:405-487) as one pass over the natural-order
-// residues with a decoupled look-back scan for the carries.
+// residues.
 //
-// Each thread turns 8 coefficients into 4 limbs; the limb carry chain is
-// resolved per warp (ballot), per block, then across blocks: a block whose
-// limbs cannot pass a carry through publishes its carry-out at once, the
-// others publish their (G, P) aggregate and look back.  Blocks take their
-// position from a ticket counter, so a block only waits on blocks already
-// running, and every wait is bounded (kSpinLimit polls, then an error bit).
+// Phase 1 (every block): each thread turns 8 coefficients into 4 limbs,
+// the limb carry chain is resolved per warp (ballot) and per block with a
+// block carry-in of 0, the limbs are written, and the block publishes its
+// aggregate (G = carry out, P = a carry-in would pass through).
+// Phase 2 (the last block to finish, found with a fence and an atomic
+// counter): scans the aggregates into per-block carry-ins and adds the
+// carry into the blocks that receive one -- on random data about one block
+// in 64, usually a single limb.  No block ever waits on another.
 #include "ntt_engine.cuh"
 
 namespace precgpu {
 
-constexpr int kSpinLimit = 1 << 20;
+constexpr int kBlockLimbs = kCarryThreads * kCarryLimbs;
 
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
+// scratch layout: [0] finished-block counter, [1 .. nblk] aggregates
+// (bit0 G, bit1 P)
 template <int SET>
 __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args) {
     __shared__ BlockCarryShared sh;
-    __shared__ uint32_t s_ticket;
-    if (threadIdx.x == 0) s_ticket = atomicAdd(&args.scratch[0], 1u);
-    __syncthreads();
-    const uint32_t bid = s_ticket;
+    __shared__ uint32_t s_last;
+    const uint32_t bid = blockIdx.x;
     const uint64_t N = 1ull << args.k;
     const uint32_t* __restrict__ r0 = args.work;
     const uint32_t* __restrict__ r1 = args.work + 2 * N;
     const uint32_t* __restrict__ r2 = args.work + 4 * N;
     const int lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)bid * (kCarryThreads * kCarryLimbs) + threadIdx.x * kCarryLimbs;
+    const int64_t m0 = (int64_t)bid * kBlockLimbs + threadIdx.x * kCarryLimbs;
     const uint64_t i0 = 2 * (uint64_t)m0;
 
     u128 T[kCarryLimbs];
@@ -85,47 +77,48 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args) {
     bool G, P;
     limbs_from_sums<kCarryLimbs>(T, prev_hi, v, gbits, G, P);
 
-    uint32_t* status = args.scratch + 1;
+    uint32_t* agg = args.scratch + 1;
     auto cin_fn = [&](bool Gb, bool Pb) -> bool {
-        // status word: bit0 aggregate ready, bit1 carry-out ready,
-        // bit2 G (or the carry-out), bit3 P
-        if (bid == 0) {
-            st_release(&status[0], 2u | (Gb ? 4u : 0u));
-            return false;
-        }
-        if (!Pb) st_release(&status[bid], 2u | (Gb ? 4u : 0u));
-        else st_release(&status[bid], 1u | (Gb ? 4u : 0u) | 8u);
-        bool accG = false, accP = true, cin = false;
-        for (int64_t j = (int64_t)bid - 1; j >= 0; --j) {
-            uint32_t s = 0;
-            int spins = 0;
-            while (((s = ld_acquire(&status[j])) & 3u) == 0) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(args.err, kDevErrTimeout);
-                    s = 2u;  // give up with carry 0; the error bit fails the product
-                    break;
-                }
-                __nanosleep(64);
-            }
-            const bool g = (s & 4u) != 0;
-            if (s & 2u) {
-                cin = accG || (accP && g);
-                break;
-            }
-            accG = accG || (accP && g);
-            accP = accP && ((s & 8u) != 0);
-        }
-        if (Pb) st_release(&status[bid], 2u | ((Gb || cin) ? 4u : 0u));
-        return cin;
+        agg[bid] = (Gb ? 1u : 0u) | (Pb ? 2u : 0u);
+        return false;
     };
     const bool cin = block_carry(G, P, sh, cin_fn);
     limbs_finish<kCarryLimbs>(m0, args.lout, v, gbits, cin, args.out);
-    if (bid + 1 == gridDim.x && threadIdx.x == blockDim.x - 1) {
-        bool c = cin;
-#pragma unroll
-        for (int k = 0; k < kCarryLimbs; ++k) c = ((gbits >> k) & 1) || (v[k] == ~0ull && c);
-        if (c) atomicOr(args.err, kDevErrCarry);  // a product never overflows La+Lb limbs
+
+    // ---- phase 2: the last block resolves the carries between blocks
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&args.scratch[0], 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int nblk = gridDim.x;
+    const int per = (nblk + blockDim.x - 1) / blockDim.x;  // aggregates per thread
+    const int b0 = threadIdx.x * per;
+    // this thread's run of blocks as one carry element
+    bool tG = false, tP = true;
+    for (int b = b0; b < b0 + per && b < nblk; ++b) {
+        const uint32_t a = __ldcg(&agg[b]);
+        tG = (a & 1u) || (tG && (a & 2u));
+        tP = tP && (a & 2u);
     }
+    auto none = [](bool, bool) -> bool { return false; };
+    bool c = block_carry(tG, tP, sh, none);  // carry into this thread's first block
+    for (int b = b0; b < b0 + per && b < nblk; ++b) {
+        const uint32_t a = __ldcg(&agg[b]);
+        if (c) {
+            // the carry enters block b: +1 ripples through its all-ones limbs
+            const uint64_t lim_end = min((uint64_t)(b + 1) * kBlockLimbs, args.lout);
+            for (uint64_t m = (uint64_t)b * kBlockLimbs; m < lim_end; ++m) {
+                const uint64_t x = __ldcg(&args.out[m]) + 1;
+                args.out[m] = x;
+                if (x != 0) break;
+            }
+        }
+        c = (a & 1u) || (c && (a & 2u));
+    }
+    // the last block's carry out must be zero: a product fits La+Lb limbs
+    if (b0 < nblk && b0 + per >= nblk && c) atomicOr(args.err, kDevErrCarry);
 }
 
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st) {

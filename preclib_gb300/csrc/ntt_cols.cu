@@ -16,7 +16,7 @@
 namespace precgpu {
 
 template <int SET, int M, int C>
-__global__ void __launch_bounds__(256) k_fwd_cols(ProdArgs args) {
+__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(256) k_fwd_cols(ProdArgs args) {
 }
 
 template <int SET, int M, int C>
-__global__ void __launch_bounds__(256) k_inv_cols(ProdArgs args) {
+__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
@@ -130,12 +130,13 @@ __global__ void __launch_bounds__(256) k_inv_cols(ProdArgs args) {
 
 // ---------------------------------------------------------------------------
 
-static int col_group(int set, int m) { return (set == 1 && m == 13) ? 4 : kColGroup; }
+// columns per CTA: 8 (32-byte sectors) while that fits three CTAs per SM
+static int col_group(int set, int m) { return (set == 1 && m >= 12) ? 4 : kColGroup; }
 
 static size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
 
 #define PREC_COLS_SET0(X) X(0, 6, 8) X(0, 7, 8) X(0, 8, 8) X(0, 9, 8) X(0, 10, 8) X(0, 11, 8)
-#define PREC_COLS_SET1(X) X(1, 12, 8) X(1, 13, 4)
+#define PREC_COLS_SET1(X) X(1, 11, 8) X(1, 12, 4) X(1, 13, 4)
 
 void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st) {
     const int m = a.k1, cg = col_group(set, m);

@@ -13,6 +13,15 @@
 #include "ntt_field.cuh"
 #include "ntt_kernels.cuh"
 
+// minimum resident 256-thread CTAs per SM the transform kernels are
+// compiled for (register budget 65536 / (256 * n))
+#ifndef PREC_ROWS_MINB
+#define PREC_ROWS_MINB 3
+#endif
+#ifndef PREC_COLS_MINB
+#define PREC_COLS_MINB 3
+#endif
+
 namespace precgpu {
 
 typedef unsigned __int128 u128;
@@ -63,18 +72,34 @@ __device__ __forceinline__ void dif_regs(uint32_t (&x)[NA][1 << RB], uint32_t ul
 #pragma unroll
     for (int bb = RB - 1; bb >= 0; --bb) {
         const int h = 1 << bb;
+        if constexpr (LO == 0) {
 #pragma unroll
-        for (int q = 0; q < (1 << RB); ++q) {
-            if (q & h) continue;
-            if (LO == 0 && (q & (h - 1)) == 0) {
+            for (int j = 0; j < h; j += 2) {
+                uint2 w0 = make_uint2(1, 0), w1 = w0;
+                if (h >= 2) {
+                    const uint4 v = __ldg(reinterpret_cast<const uint4*>(tw + (1u << bb) + j));
+                    w0 = make_uint2(v.x, v.y);
+                    w1 = make_uint2(v.z, v.w);
+                }
 #pragma unroll
-                for (int a = 0; a < NA; ++a) Ar<SET>::dif1(x[a][q], x[a][q + h], c);
-                continue;
+                for (int q0 = 0; q0 < (1 << RB); q0 += 2 * h) {
+#pragma unroll
+                    for (int a = 0; a < NA; ++a) {
+                        if (j == 0) Ar<SET>::dif1(x[a][q0], x[a][q0 + h], c);
+                        else Ar<SET>::dif(x[a][q0 + j], x[a][q0 + j + h], w0, c);
+                        if (h >= 2) Ar<SET>::dif(x[a][q0 + j + 1], x[a][q0 + j + 1 + h], w1, c);
+                    }
+                }
             }
-            const uint32_t j = (LO == 0 ? 0u : ulo) | ((uint32_t)(q & (h - 1)) << LO);
-            const uint2 w = __ldg(&tw[(1u << (LO + bb)) + j]);
+        } else {
 #pragma unroll
-            for (int a = 0; a < NA; ++a) Ar<SET>::dif(x[a][q], x[a][q + h], w, c);
+            for (int q = 0; q < (1 << RB); ++q) {
+                if (q & h) continue;
+                const uint32_t j = ulo | ((uint32_t)(q & (h - 1)) << LO);
+                const uint2 w = __ldg(&tw[(1u << (LO + bb)) + j]);
+#pragma unroll
+                for (int a = 0; a < NA; ++a) Ar<SET>::dif(x[a][q], x[a][q + h], w, c);
+            }
         }
     }
 }
@@ -86,18 +111,34 @@ __device__ __forceinline__ void dit_regs(uint32_t (&x)[NA][1 << RB], uint32_t ul
 #pragma unroll
     for (int bb = 0; bb < RB; ++bb) {
         const int h = 1 << bb;
+        if constexpr (LO == 0) {
 #pragma unroll
-        for (int q = 0; q < (1 << RB); ++q) {
-            if (q & h) continue;
-            if (LO == 0 && (q & (h - 1)) == 0) {
+            for (int j = 0; j < h; j += 2) {
+                uint2 w0 = make_uint2(1, 0), w1 = w0;
+                if (h >= 2) {
+                    const uint4 v = __ldg(reinterpret_cast<const uint4*>(tw + (1u << bb) + j));
+                    w0 = make_uint2(v.x, v.y);
+                    w1 = make_uint2(v.z, v.w);
+                }
 #pragma unroll
-                for (int a = 0; a < NA; ++a) Ar<SET>::dit1(x[a][q], x[a][q + h], c);
-                continue;
+                for (int q0 = 0; q0 < (1 << RB); q0 += 2 * h) {
+#pragma unroll
+                    for (int a = 0; a < NA; ++a) {
+                        if (j == 0) Ar<SET>::dit1(x[a][q0], x[a][q0 + h], c);
+                        else Ar<SET>::dit(x[a][q0 + j], x[a][q0 + j + h], w0, c);
+                        if (h >= 2) Ar<SET>::dit(x[a][q0 + j + 1], x[a][q0 + j + 1 + h], w1, c);
+                    }
+                }
             }
-            const uint32_t j = (LO == 0 ? 0u : ulo) | ((uint32_t)(q & (h - 1)) << LO);
-            const uint2 w = __ldg(&tw[(1u << (LO + bb)) + j]);
+        } else {
 #pragma unroll
-            for (int a = 0; a < NA; ++a) Ar<SET>::dit(x[a][q], x[a][q + h], w, c);
+            for (int q = 0; q < (1 << RB); ++q) {
+                if (q & h) continue;
+                const uint32_t j = ulo | ((uint32_t)(q & (h - 1)) << LO);
+                const uint2 w = __ldg(&tw[(1u << (LO + bb)) + j]);
+#pragma unroll
+                for (int a = 0; a < NA; ++a) Ar<SET>::dit(x[a][q], x[a][q + h], w, c);
+            }
         }
     }
 }

@@ -12,7 +12,7 @@
 namespace precgpu {
 
 template <int SET, int M>
-__global__ void __launch_bounds__(256) k_rows(ProdArgs args) {
+__global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "row transforms have at least two passes");
@@ -117,7 +117,7 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
     return rows << (k2 - 5);
 }
 
-#define PREC_ROWS(X) X(0, 7) X(0, 8) X(0, 9) X(0, 10) X(0, 11) X(0, 12) X(1, 12) X(1, 13)
+#define PREC_ROWS(X) X(0, 7) X(0, 8) X(0, 9) X(0, 10) X(0, 11) X(0, 12) X(1, 13)
 
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st) {
     const int m = a.k2;

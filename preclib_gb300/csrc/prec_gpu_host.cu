@@ -114,7 +114,9 @@ static int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
         return 0;
     }
     pl.path = 1;
-    pl.k1 = k / 2;
+    // column length N1 = 2^k1, row length N2 = 2^k2; set 1 keeps the rows
+    // at 2^13 so its column CTAs stay within a third of shared memory
+    pl.k1 = pl.set == 0 ? k / 2 : k - 13;
     pl.k2 = k - pl.k1;
     ntt_row_threads(pl.k2, 1 << pl.k1, &pl.rows);
     const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;

@@ -78,6 +78,20 @@ def test_all_ones_maximal_carries(gpu):
         assert np.array_equal(got, want), n
 
 
+@pytest.mark.parametrize("n,k", [(3000, 1500), (5000, 1024), (9000, 4096), (70000, 30001), (1 << 20, 1 << 19)])
+def test_all_ones_runs_across_carry_blocks(gpu, n, k):
+    """(2^(64n)-1) * (2^(64k)+1) and (2^(64n)-1) * 2^(64k): results with
+    all-ones runs spanning many 1024-limb carry blocks."""
+    a = np.full(n, 0xFFFFFFFFFFFFFFFF, dtype=np.uint64)
+    b = np.zeros(k + 1, np.uint64)
+    b[0] = 1
+    b[k] = 1
+    want = O.to_int(a) * O.to_int(b)
+    assert O.to_int(gpu.mul(a, b, ntt=True)) == want
+    b[0] = 0
+    assert O.to_int(gpu.mul(a, b, ntt=True)) == O.to_int(a) << (64 * k)
+
+
 def test_torture_ntt(gpu):
     for (an, bn) in patterns.TORTURE_SHAPES:
         for p in patterns.TORTURE_PATTERNS:

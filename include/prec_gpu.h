@@ -89,6 +89,23 @@ int prec_gpu_mul_device_profile(const uint64_t *d_a, size_t an, const uint64_t *
 /* Kernel name of stage `stage` of path `path` ("" if out of range). */
 const char *prec_gpu_stage_name(int path, int stage);
 
+/* The product of prec_gpu_mul_device for callers that cannot allocate device
+ * memory (their memory is owned by their own pool allocator, they cannot
+ * accept the device-wide synchronisation that cudaFree implies, or their
+ * host forbids allocation after start-up).  No counterpart in the
+ * reference.  Allocates nothing: the caller passes inputs and output on
+ * the device; all other memory is a fixed array inside the library
+ * (about 6.6 MiB, held by every device that loads the library until the
+ * process exits).  Limit: an + bn <= 131072 limbs (transforms up to 2^18
+ * points); larger products return PREC_GPU_E_TOO_LARGE.  The first call on
+ * a device sets that device up (fills the library's twiddle tables with a
+ * kernel on `stream` and waits for it), so make the first call before any
+ * stream capture.  Calls share the one array: calls that overlap on the
+ * GPU (other streams, other threads) race and corrupt each other's result;
+ * serialise them.  Asynchronous otherwise; it reports launch errors only. */
+int prec_gpu_mul_device_noalloc(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
+                                uint64_t *d_out, void *stream);
+
 /* Synchronises `stream` and reports any device-side error raised by work
  * the library enqueued (PREC_GPU_E_TIMEOUT, PREC_GPU_E_INTERNAL) or a
  * CUDA error. */

@@ -22,7 +22,7 @@ EXPORTS = (
     "prec_gpu_init", "prec_gpu_shutdown", "prec_gpu_mul", "prec_gpu_mul_ntt",
     "prec_gpu_mul_device", "prec_gpu_stream_check", "prec_gpu_last_stats",
     "prec_gpu_ntt_log2", "prec_gpu_strerror", "prec_gpu_mul_device_profile",
-    "prec_gpu_stage_name",
+    "prec_gpu_stage_name", "prec_gpu_mul_device_noalloc",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -72,6 +72,9 @@ def lib() -> ctypes.CDLL:
                                                   ctypes.POINTER(ctypes.c_float),
                                                   ctypes.POINTER(ctypes.c_int)]
         L.prec_gpu_mul_device_profile.restype = ctypes.c_int
+        L.prec_gpu_mul_device_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                                  ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+        L.prec_gpu_mul_device_noalloc.restype = ctypes.c_int
         L.prec_gpu_stage_name.argtypes = [ctypes.c_int, ctypes.c_int]
         L.prec_gpu_stage_name.restype = ctypes.c_char_p
         L.prec_gpu_strerror.argtypes = [ctypes.c_int]

@@ -68,6 +68,18 @@ int prec_gpu_mul(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uin
 /* NTT band forced, host pointers (replaces mul_ntt, src/mul_ntt.cpp:494). */
 int prec_gpu_mul_ntt(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uint64_t *out);
 
+/* FP64 FFT band forced, host pointers (replaces mul_fft, src/mul_fft.cpp:386).
+ * Products with max(an,bn) <= 6144 limbs run the FP64 FFT: balanced digits
+ * of the widest width (16 .. 8 bits) whose worst-case rounding bound stays
+ * below 1/4; the product's max distance to the nearest integer is reported
+ * in prec_gpu_stats_t.fft_max_distance, and a distance above 0.25 returns
+ * PREC_GPU_E_FFT_ROUNDING with `out` untouched.  Larger products (squares
+ * that precn_sqr sends to mul_fft, src/mul_basic.cpp:203) run the NTT band. */
+int prec_gpu_mul_fft(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uint64_t *out);
+
+/* Digit width (bits) the FP64 band uses for an x bn limbs; 0 outside the band. */
+int prec_gpu_fft_digit_bits(size_t an, size_t bn);
+
 /* Same product on device pointers, enqueued on `stream` (a cudaStream_t;
  * NULL = legacy default stream) without host synchronisation.  Operands
  * stay as given (no trimming of zero high limbs).  The call returns after

@@ -1,0 +1,345 @@
+// fft_kernels.cu -- FP64 FFT band (193 .. 6144 limbs) of the multiply.
+//
+// Replaces preclib's mul_fft (src/mul_fft.cpp:340-394) with the same method
+// -- both operands packed as the real and imaginary parts of one complex
+// FP64 FFT (fft_load_digits, 234-246), the two spectra separated and
+// multiplied (fft_pair_convolution, 248-305), one inverse FFT, rounding to
+// the nearest integer (307-309, 364-376) and a signed carry back to limbs
+// (fft_from_digits, 311-338) -- laid out for many SMs:
+//
+//  digits   balanced b-bit digits (|d| <= 2^(b-1)), b chosen per transform
+//           length from a worst-case error bound (host side); every digit
+//           is computed on its own: d_i = raw_i - 2^b t_i + t_{i-1} with
+//           t_j = [raw_j >= 2^(b-1)], so no carry chain is needed.
+//  twiddles one table of e^(2 pi i e / 2^16), e < 2^15, from sincospi()
+//           (the reference builds per-stage tables by a recurrence,
+//           mul_fft.cpp:57-76).
+//  four-step N = N1 * N2:
+//    k_fft_fwd_cols  digits -> column DIF over i1 -> twiddle w^-(i2 k1)
+//    k_fft_rows      rows k1 and N1-k1 together: row DIF, separation and
+//                    product (P_-k = conj P_k), row DIT, twiddle w^(i2 k1)
+//    k_fft_inv_cols  column DIT -> x/N -> nearest integer, max distance
+//    k_fft_carry     one CTA: limbs from the signed coefficients; writes
+//                    nothing when the max distance exceeds 0.25.
+#include <cuda_runtime.h>
+
+#include "fft_kernels.cuh"
+
+namespace precgpu {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -a.y); }
+
+// w_N^e = e^(2 pi i e / N) for 0 <= e < N, N = 2^k <= 2^16
+__device__ __forceinline__ double2 root(const double2* __restrict__ tw, uint32_t e, int k) {
+    const uint32_t half = 1u << (k - 1);
+    const double2 w = __ldg(&tw[(e & (half - 1)) << (kFftMaxLog2 - k)]);
+    return (e & half) ? make_double2(-w.x, -w.y) : w;
+}
+
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 4); }  // 16-byte elements, 1 spare per 16
+
+// raw b-bit digit i of an n-limb operand (zero past its top)
+__device__ __forceinline__ uint32_t raw_digit(const uint64_t* __restrict__ a, uint64_t n, int b, uint64_t i) {
+    const uint64_t bit = (uint64_t)b * i;
+    const uint64_t limb = bit >> 6;
+    const int sh = (int)(bit & 63);
+    uint64_t v = limb < n ? __ldg(&a[limb]) >> sh : 0;
+    if (sh + b > 64 && limb + 1 < n) v |= __ldg(&a[limb + 1]) << (64 - sh);
+    return (uint32_t)(v & ((1ull << b) - 1));
+}
+
+// balanced digit i (|d| <= 2^(b-1)) of an operand with `nd` digits
+__device__ __forceinline__ double bal_digit(const uint64_t* __restrict__ a, uint64_t n, int b, uint64_t i, uint64_t nd) {
+    if (i >= nd) return 0.0;
+    const uint32_t half = 1u << (b - 1);
+    const uint32_t r = raw_digit(a, n, b, i);
+    const int t_in = i > 0 && raw_digit(a, n, b, i - 1) >= half ? 1 : 0;
+    const int t_out = r >= half ? 1 : 0;
+    return (double)((int64_t)r - ((int64_t)t_out << b) + t_in);
+}
+
+// radix-2 stages over `narr` arrays of 2^m points in shared memory (array
+// stride `as` elements, element i at fpad(i)); sign -1 forward (DIF,
+// natural -> bit-reversed), +1 inverse (DIT, bit-reversed -> natural)
+template <bool DIT>
+__device__ void fft_stages(double2* s, int as, int narr, int m, const double2* __restrict__ tw) {
+    const int half_n = 1 << (m - 1);
+    for (int st = 0; st < m; ++st) {
+        const int bb = DIT ? st : m - 1 - st;  // paired index bit
+        const int h = 1 << bb;
+        for (int w = threadIdx.x; w < narr * half_n; w += blockDim.x) {
+            const int a = w / half_n, p = w % half_n;
+            const int j = p & (h - 1);
+            const int i0 = ((p >> bb) << (bb + 1)) | j;
+            double2* x = s + a * as + fpad(i0);
+            double2* y = s + a * as + fpad(i0 + h);
+            // w_{2h}^{+-j}
+            double2 r = root(tw, (uint32_t)j << (m - 1 - bb), m);
+            if (!DIT) r.y = -r.y;
+            const double2 xv = *x, yv = *y;
+            if (DIT) {
+                const double2 t = j ? cmul(yv, r) : yv;
+                *x = cadd(xv, t);
+                *y = csub(xv, t);
+            } else {
+                *x = cadd(xv, yv);
+                const double2 d = csub(xv, yv);
+                *y = j ? cmul(d, r) : d;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ uint32_t bitrev(uint32_t x, int bits) { return bits ? __brev(x) >> (32 - bits) : 0u; }
+
+// forward column pass: grid N2/C CTAs, C adjacent columns each
+template <int C>
+__global__ void __launch_bounds__(256) k_fft_fwd_cols(FftArgs f) {
+    extern __shared__ double2 fsm[];
+    const int N1 = 1 << f.k1;
+    const uint32_t N2 = 1u << f.k2;
+    const int as = fpad(N1) + 1;
+    const uint32_t c0 = blockIdx.x * C;
+    for (int w = threadIdx.x; w < C * N1; w += blockDim.x) {
+        const int col = w % C, i1 = w / C;
+        const uint64_t i = (uint64_t)i1 * N2 + c0 + col;
+        fsm[col * as + fpad(i1)] = make_double2(bal_digit(f.a, f.la, f.b, i, f.da), bal_digit(f.bp, f.lb, f.b, i, f.db));
+    }
+    __syncthreads();
+    fft_stages<false>(fsm, as, C, f.k1, f.tw);
+    for (int w = threadIdx.x; w < C * N1; w += blockDim.x) {
+        const int col = w % C, s = w / C;
+        const uint32_t k1 = bitrev((uint32_t)s, f.k1);
+        const uint32_t i2 = c0 + col;
+        double2 r = root(f.tw, (i2 * k1) & ((1u << f.k) - 1), f.k);
+        r.y = -r.y;
+        f.work[(uint64_t)s * N2 + i2] = cmul(fsm[col * as + fpad(s)], r);
+    }
+}
+
+// row pass: CTA r handles frequency rows k1 = r and N1 - r (one row when
+// they coincide); grid N1/2 + 1
+__global__ void __launch_bounds__(256) k_fft_rows(FftArgs f) {
+    extern __shared__ double2 fsm[];
+    const int N1 = 1 << f.k1, N2 = 1 << f.k2;
+    const int as = fpad(N2) + 1;
+    const uint32_t ka = blockIdx.x, kb = (N1 - blockIdx.x) & (N1 - 1);
+    const int nrow = ka == kb ? 1 : 2;
+    const uint32_t sa = bitrev(ka, f.k1), sb = bitrev(kb, f.k1);
+    double2* rowp[2] = {f.work + (uint64_t)sa * N2, f.work + (uint64_t)sb * N2};
+    for (int w = threadIdx.x; w < nrow * N2; w += blockDim.x) {
+        const int r = w / N2, t = w % N2;
+        fsm[r * as + fpad(t)] = rowp[r][t];
+    }
+    __syncthreads();
+    fft_stages<false>(fsm, as, nrow, f.k2, f.tw);
+    // separation of the packed spectra and product; slot t holds k2 = bitrev(t)
+    double2 prod[8];  // at most 2 * N2 / blockDim = 8 elements per thread
+    int cnt = 0;
+    for (int w = threadIdx.x; w < nrow * N2; w += blockDim.x, ++cnt) {
+        const int r = w / N2, t = w % N2;
+        const uint32_t k1 = r ? kb : ka;
+        const uint32_t k2 = bitrev((uint32_t)t, f.k2);
+        const uint32_t pk2 = (N2 - k2 - (k1 != 0 ? 1u : 0u)) & (N2 - 1);
+        const int pr = (nrow == 1) ? 0 : 1 - r;  // the partner row
+        const double2 F = fsm[r * as + fpad(t)];
+        const double2 G = conj2(fsm[pr * as + fpad(bitrev(pk2, f.k2))]);  // conj(F_-k)
+        const double2 A = make_double2(0.5 * (F.x + G.x), 0.5 * (F.y + G.y));
+        // B = (F - conj F_-k) / 2i
+        const double2 D = csub(F, G);
+        const double2 B = make_double2(0.5 * D.y, -0.5 * D.x);
+        prod[cnt] = cmul(A, B);
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int w = threadIdx.x; w < nrow * N2; w += blockDim.x, ++cnt) {
+        const int r = w / N2, t = w % N2;
+        fsm[r * as + fpad(t)] = prod[cnt];
+    }
+    __syncthreads();
+    fft_stages<true>(fsm, as, nrow, f.k2, f.tw);
+    for (int w = threadIdx.x; w < nrow * N2; w += blockDim.x) {
+        const int r = w / N2, i2 = w % N2;
+        const uint32_t k1 = r ? kb : ka;
+        const double2 rt = root(f.tw, (i2 * k1) & ((1u << f.k) - 1), f.k);
+        rowp[r][i2] = cmul(fsm[r * as + fpad(i2)], rt);
+    }
+}
+
+// inverse column pass, scaling, rounding; grid N2/C
+template <int C>
+__global__ void __launch_bounds__(256) k_fft_inv_cols(FftArgs f) {
+    extern __shared__ double2 fsm[];
+    __shared__ double s_max[8];
+    const int N1 = 1 << f.k1;
+    const uint32_t N2 = 1u << f.k2;
+    const int as = fpad(N1) + 1;
+    const uint32_t c0 = blockIdx.x * C;
+    for (int w = threadIdx.x; w < C * N1; w += blockDim.x) {
+        const int col = w % C, s = w / C;
+        fsm[col * as + fpad(s)] = f.work[(uint64_t)s * N2 + c0 + col];
+    }
+    __syncthreads();
+    fft_stages<true>(fsm, as, C, f.k1, f.tw);
+    const double inv_n = 1.0 / (double)(1u << f.k);
+    double dmax = 0.0;
+    for (int w = threadIdx.x; w < C * N1; w += blockDim.x) {
+        const int col = w % C, i1 = w / C;
+        const double v = fsm[col * as + fpad(i1)].x * inv_n;
+        const double r = rint(v);
+        double d = fabs(v - r);
+        if (!isfinite(v)) d = INFINITY;
+        dmax = fmax(dmax, d);
+        f.coef[(uint64_t)i1 * N2 + c0 + col] = (long long)r;
+    }
+    for (int o = 16; o > 0; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = dmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) dmax = fmax(dmax, s_max[i]);
+        // non-negative doubles order like their bit patterns
+        atomicMax(reinterpret_cast<unsigned long long*>(f.maxdist), (unsigned long long)__double_as_longlong(dmax));
+    }
+}
+
+// signed carry: one CTA of 1024 threads, limbs of the product from the
+// rounded coefficients c_i (value sum c_i 2^(b i)).  A limb's sum
+// S_m = sum of c_i 2^(b i - 64 m) over the coefficients starting in it is a
+// signed 128-bit value; v_m = lo64(S_m) + hi(S_{m-1}) = u_m + g_m 2^64 with
+// g_m in {-1, 0, 1}, and the carry chain c_{m+1} = g_m + floor((u_m + c_m)
+// / 2^64) stays in {-1, 0, 1}.  Each thread composes the chain of its limbs
+// into a map {-1,0,1} -> {-1,0,1}; the block scans the maps.
+typedef __int128 i128;
+
+__device__ __forceinline__ i128 limb_sum_s(const long long* __restrict__ c, uint64_t ncoef, int b, int64_t m) {
+    if (m < 0) return 0;
+    const uint64_t lo_bit = (uint64_t)m * 64;
+    uint64_t i = (lo_bit + b - 1) / b;
+    i128 s = 0;
+    for (; i < ncoef && (uint64_t)b * i < lo_bit + 64; ++i)
+        s += (i128)((unsigned __int128)(i128)c[i] << ((uint64_t)b * i - lo_bit));  // two's complement shift
+    return s;
+}
+
+__device__ __forceinline__ int chain_step(uint64_t u, int g, int cin, uint64_t* out_limb) {
+    const uint64_t r = u + (uint64_t)(int64_t)cin;
+    if (out_limb) *out_limb = r;
+    int fl = 0;
+    if (cin < 0 && u == 0) fl = -1;
+    if (cin > 0 && u == ~0ull) fl = 1;
+    return g + fl;
+}
+
+__global__ void __launch_bounds__(1024) k_fft_carry(FftArgs f) {
+    __shared__ uint8_t maps[2][1024][3];
+    const double dist = *f.maxdist;
+    if (!(dist <= 0.25)) {  // also NaN / inf
+        if (threadIdx.x == 0) atomicOr(f.err, kDevErrFftRound);
+        return;
+    }
+    // Balanced digits can place signed contributions past the product's
+    // La+Lb limbs (they cancel a borrow that runs up to them), so the chain
+    // covers every limb a coefficient reaches; those limbs must end as 0.
+    const int64_t Lout = (int64_t)f.lout;
+    const int64_t Lcoef = (int64_t)(((uint64_t)f.b * f.ncoef + 63) / 64) + 2;
+    const int64_t L = Lcoef > Lout ? Lcoef : Lout;
+    const int64_t per = (L + blockDim.x - 1) / blockDim.x;
+    const int64_t m0 = (int64_t)threadIdx.x * per;
+    const int64_t m1 = m0 + per < L ? m0 + per : L;
+    // this thread's chain as a map of the carry-in (index cin + 1)
+    int out_of[3];
+    for (int cin = -1; cin <= 1; ++cin) {
+        int c = cin;
+        i128 prev = limb_sum_s(f.coef, f.ncoef, f.b, m0 - 1);
+        for (int64_t m = m0; m < m1; ++m) {
+            const i128 cur = limb_sum_s(f.coef, f.ncoef, f.b, m);
+            const i128 v = (i128)(uint64_t)cur + (prev >> 64);
+            c = chain_step((uint64_t)v, (int)(v >> 64), c, nullptr);
+            prev = cur;
+        }
+        out_of[cin + 1] = c < -1 ? -1 : (c > 1 ? 1 : c);
+    }
+    int buf = 0;
+    for (int q = 0; q < 3; ++q) maps[0][threadIdx.x][q] = (uint8_t)(out_of[q] + 1);
+    __syncthreads();
+    // inclusive scan of maps: M_t = f_t o f_{t-1} o ... o f_0
+    for (int d = 1; d < (int)blockDim.x; d <<= 1) {
+        uint8_t nm[3];
+        for (int q = 0; q < 3; ++q) {
+            const uint8_t mine = maps[buf][threadIdx.x][q];
+            nm[q] = mine;
+            if ((int)threadIdx.x >= d) nm[q] = maps[buf][threadIdx.x][maps[buf][threadIdx.x - d][q]];
+        }
+        for (int q = 0; q < 3; ++q) maps[buf ^ 1][threadIdx.x][q] = nm[q];
+        __syncthreads();
+        buf ^= 1;
+    }
+    // carry into this thread's first limb: prefix map of threads < t applied to 0
+    int c = threadIdx.x == 0 ? 0 : (int)maps[buf][threadIdx.x - 1][1] - 1;
+    i128 prev = limb_sum_s(f.coef, f.ncoef, f.b, m0 - 1);
+    for (int64_t m = m0; m < m1; ++m) {
+        const i128 cur = limb_sum_s(f.coef, f.ncoef, f.b, m);
+        const i128 v = (i128)(uint64_t)cur + (prev >> 64);
+        uint64_t limb;
+        c = chain_step((uint64_t)v, (int)(v >> 64), c, &limb);
+        if (m < Lout) f.out[m] = limb;
+        else if (limb != 0) atomicOr(f.err, kDevErrCarry);  // a product fits La+Lb limbs
+        prev = cur;
+    }
+    if (m0 < L && m1 == L && c != 0) atomicOr(f.err, kDevErrCarry);
+}
+
+// e^(2 pi i e / 2^16) for e < 2^15
+__global__ void k_fft_table(double2* tw) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < (1 << (kFftMaxLog2 - 1))) {
+        double s, c;
+        sincospi((double)e / (double)(1 << (kFftMaxLog2 - 1)), &s, &c);
+        tw[e] = make_double2(c, s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+
+constexpr int kFftCols = 2;
+
+size_t fft_table_bytes() { return (size_t)sizeof(double2) << (kFftMaxLog2 - 1); }
+
+void fft_build_table(double2* tw, cudaStream_t st) {
+    k_fft_table<<<(1 << (kFftMaxLog2 - 1)) / 256, 256, 0, st>>>(tw);
+}
+
+static size_t cols_smem(int k1) { return (size_t)kFftCols * (fpad_host(1 << k1) + 1) * sizeof(double2); }
+static size_t rows_smem(int k2) { return (size_t)2 * (fpad_host(1 << k2) + 1) * sizeof(double2); }
+
+int fft_configure_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_fft_fwd_cols<kFftCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)cols_smem(kFftMaxLog2 / 2));
+    if (!e) e = cudaFuncSetAttribute(k_fft_inv_cols<kFftCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cols_smem(kFftMaxLog2 / 2));
+    if (!e) e = cudaFuncSetAttribute(k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)rows_smem(kFftMaxLog2 - kFftMaxLog2 / 2));
+    return (int)e;
+}
+
+void fft_launch(const FftArgs& f, cudaStream_t st, cudaEvent_t* ev) {
+    if (ev) cudaEventRecord(ev[0], st);
+    cudaMemsetAsync(f.maxdist, 0, sizeof(double), st);
+    const int ncol = (1 << f.k2) / kFftCols;
+    k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
+    if (ev) cudaEventRecord(ev[1], st);
+    k_fft_rows<<<(1 << f.k1) / 2 + 1, 256, rows_smem(f.k2), st>>>(f);
+    if (ev) cudaEventRecord(ev[2], st);
+    k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
+    if (ev) cudaEventRecord(ev[3], st);
+    k_fft_carry<<<1, 1024, 0, st>>>(f);
+    if (ev) cudaEventRecord(ev[4], st);
+}
+
+}  // namespace precgpu

@@ -11,12 +11,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
 
 #include "../../include/prec_gpu.h"
+#include "fft_kernels.cuh"
 #include "ntt_kernels.cuh"
 
 namespace precgpu {
@@ -67,6 +70,10 @@ static const char* const kStageNames[3][kMaxStages] = {
     {"k_fft"},
 };
 static const int kStageCount[3] = {1, 4, 1};
+
+constexpr size_t kStatBytes = 16;       // device status block (error bits, FFT distance)
+constexpr size_t kFftBandMin = 192;     // src/mul_basic.cpp:4 (FFT above 192 limbs)
+constexpr size_t kFftBandMax = 6144;    // src/mul_basic.cpp:5 (NTT above 6144 limbs)
 
 struct Plan {
     int k = 0, k1 = 0, k2 = 0;
@@ -135,8 +142,11 @@ struct Ctx {
     size_t ws_cap = 0;
     uint64_t* io = nullptr;
     size_t io_cap = 0;  // limbs
-    int* d_err = nullptr;
-    int* h_err = nullptr;
+    int* d_err = nullptr;      // device status: error bits at +0, FFT max distance at +8
+    int* h_err = nullptr;      // pinned copy of the status
+    double* d_maxdist = nullptr;
+    double* h_maxdist = nullptr;
+    double2* fft_tw = nullptr;  // FP64 band twiddles
     cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t stage_ev[kMaxStages + 1] = {};
     FieldArgs field[kSets] = {};
@@ -236,10 +246,16 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
     for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&c.stage_ev[i]));
-    CK(cudaMalloc(&c.d_err, sizeof(int)));
-    CK(cudaMemset(c.d_err, 0, sizeof(int)));
-    CK(cudaMallocHost(&c.h_err, sizeof(int)));
+    CK(cudaMalloc(&c.d_err, kStatBytes));
+    CK(cudaMemset(c.d_err, 0, kStatBytes));
+    CK(cudaMallocHost(&c.h_err, kStatBytes));
+    c.d_maxdist = reinterpret_cast<double*>(reinterpret_cast<char*>(c.d_err) + 8);
+    c.h_maxdist = reinterpret_cast<double*>(reinterpret_cast<char*>(c.h_err) + 8);
     CK((cudaError_t)ntt_configure_kernels());
+    CK((cudaError_t)fft_configure_kernels());
+    CK(cudaMalloc(&c.fft_tw, fft_table_bytes()));
+    fft_build_table(c.fft_tw, c.stream);
+    CK(cudaGetLastError());
     int r = build_tables(c);
     if (r) return r;
     CK(cudaDeviceSynchronize());
@@ -334,7 +350,63 @@ static uint64_t digits32(const uint64_t* a, size_t n) {  // n > 0, a[n-1] != 0
     return 2 * (uint64_t)n - ((a[n - 1] >> 32) == 0 ? 1 : 0);
 }
 
-static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
+// ---------------------------------------------------------------------------
+// FP64 FFT band plan
+// ---------------------------------------------------------------------------
+
+// Worst-case rounding error of a 2^k-point FP64 convolution of b-bit
+// balanced digits: C. Percival, "Rapid multiplication modulo the sum and
+// difference of highly composite numbers", Math. Comp. 72 (2003), Thm 5.1:
+// |err| <= |x| |y| ((1+e)^3k (1+e sqrt5)^(3k+1) (1+beta)^3k - 1), with
+// |x| |y| <= N 2^(2b-2), e = 2^-53 and beta = 2^-52 for sincospi twiddles;
+// doubled because both operands share one complex transform.
+static double fft_error_bound(int b, int k) {
+    const double e = std::ldexp(1.0, -53), beta = std::ldexp(1.0, -52);
+    const double g = std::expm1(3.0 * k * std::log1p(e) + (3.0 * k + 1) * std::log1p(e * std::sqrt(5.0)) +
+                                3.0 * k * std::log1p(beta));
+    return 2.0 * std::ldexp(1.0, k + 2 * b - 2) * g;
+}
+
+struct FftPlan {
+    int b = 0, k = 0, k1 = 0, k2 = 0;
+    uint64_t da = 0, db = 0;
+    size_t work_bytes = 0;
+};
+
+// Test knob for the rounding-failure path: PREC_GPU_FFT_DIGIT_BITS=b (8..30)
+// forces the digit width regardless of the bound, so a test can make the
+// FP64 band exceed 1/4 and check that the product is refused.
+static int fft_forced_bits() {
+    const char* s = std::getenv("PREC_GPU_FFT_DIGIT_BITS");
+    if (!s) return 0;
+    const int b = std::atoi(s);
+    return b >= 8 && b <= 30 ? b : 0;
+}
+
+// widest digit (16 .. 8 bits) whose bound stays below 1/4
+static bool fft_plan_for(uint64_t la, uint64_t lb, FftPlan& fp) {
+    const int forced = fft_forced_bits();
+    for (int b = forced ? forced : 16; b >= 8; --b) {
+        const uint64_t da = (64 * la + b - 1) / b + 1, db = (64 * lb + b - 1) / b + 1;
+        int k = 6;
+        while ((1ull << k) < da + db - 1) ++k;
+        if (k > kFftMaxLog2) continue;
+        if (!forced && fft_error_bound(b, k) >= 0.25) continue;
+        fp.b = b;
+        fp.k = k;
+        fp.k1 = k / 2;
+        fp.k2 = k - fp.k1;
+        fp.da = da;
+        fp.db = db;
+        fp.work_bytes = ((size_t)sizeof(double2) + sizeof(long long)) << k;
+        return true;
+    }
+    return false;
+}
+
+enum { kModeBands = 0, kModeNtt = 1, kModeFft = 2 };
+
+static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out, int mode) {
     if ((!a && an) || (!b && bn) || (!out && an + bn)) return PREC_GPU_E_ARG;
     Ctx& c = g_ctx;
     std::lock_guard<std::mutex> lk(c.mu);
@@ -350,9 +422,16 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         return 0;
     }
     const uint64_t lout = la + lb;
+    const size_t hi = la > lb ? la : lb;
+    // band routing of src/mul_basic.cpp:263-269: 193..6144 limbs -> FP64 FFT;
+    // larger products (and squares reaching mul_fft above 6144 limbs) and
+    // products below 193 limbs -> NTT
+    FftPlan fp;
+    const bool use_fft = ((mode == kModeBands && hi > kFftBandMin) || mode == kModeFft) && hi <= kFftBandMax &&
+                         fft_plan_for(la, lb, fp);
     Plan pl;
-    if ((r = plan_for(digits32(a, la), digits32(b, lb), lout, pl))) return r;
-    if ((r = ensure_ws(c, pl.work_bytes))) return r;
+    if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl))) return r;
+    if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
     if ((r = ensure_io(c, 2 * lout))) return r;
     uint64_t* d_a = c.io;
     uint64_t* d_b = c.io + la;
@@ -362,19 +441,48 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     CK(cudaMemcpyAsync(d_a, a, la * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(c.ev0, st));
-    if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st))) return r;
+    if (use_fft) {
+        FftArgs f{};
+        f.a = d_a;
+        f.bp = d_b;
+        f.out = d_out;
+        f.work = reinterpret_cast<double2*>(c.ws);
+        f.coef = reinterpret_cast<long long*>(c.ws + (sizeof(double2) << fp.k));
+        f.maxdist = c.d_maxdist;
+        f.err = c.d_err;
+        f.tw = c.fft_tw;
+        f.la = la;
+        f.lb = lb;
+        f.lout = lout;
+        f.da = fp.da;
+        f.db = fp.db;
+        f.ncoef = 1ull << fp.k;
+        f.b = fp.b;
+        f.k = fp.k;
+        f.k1 = fp.k1;
+        f.k2 = fp.k2;
+        fft_launch(f, st);
+        CK(cudaGetLastError());
+    } else if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st))) {
+        return r;
+    }
     CK(cudaEventRecord(c.ev1, st));
-    CK(cudaMemcpyAsync(out, d_out, lout * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(c.h_err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    // error word and the FFT distance first: a failed product leaves `out` untouched
+    CK(cudaMemcpyAsync(c.h_err, c.d_err, kStatBytes, cudaMemcpyDeviceToHost, st));
     CK(cudaMemsetAsync(c.d_err, 0, sizeof(int), st));
+    if (use_fft) CK(cudaStreamSynchronize(st));
+    const bool fft_failed = use_fft && (*c.h_err & kDevErrFftRound);
+    if (!fft_failed) CK(cudaMemcpyAsync(out, d_out, lout * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(c.last_done, st));
     CK(cudaStreamSynchronize(st));
-    if (total > lout) memset(out + lout, 0, (total - lout) * sizeof(uint64_t));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
-    t_stats.path = pl.path;
-    t_stats.log2_n = pl.k;
+    t_stats.path = use_fft ? 2 : pl.path;
+    t_stats.log2_n = use_fft ? fp.k : pl.k;
     t_stats.device_ms = ms;
+    t_stats.fft_max_distance = use_fft ? *c.h_maxdist : 0.0;
+    if (fft_failed) return PREC_GPU_E_FFT_ROUNDING;
+    if (total > lout) memset(out + lout, 0, (total - lout) * sizeof(uint64_t));
     if (*c.h_err & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
     if (*c.h_err) return PREC_GPU_E_INTERNAL;
     return 0;
@@ -399,6 +507,7 @@ void prec_gpu_shutdown(void) {
     cudaFree(c.ws);
     cudaFree(c.io);
     cudaFree(c.tables);
+    cudaFree(c.fft_tw);
     cudaFree(c.d_err);
     cudaFreeHost(c.h_err);
     cudaEventDestroy(c.last_done);
@@ -414,11 +523,21 @@ void prec_gpu_shutdown(void) {
 }
 
 int prec_gpu_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
-    return host_mul(a, an, b, bn, out);
+    return host_mul(a, an, b, bn, out, kModeBands);
 }
 
 int prec_gpu_mul_ntt(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
-    return host_mul(a, an, b, bn, out);
+    return host_mul(a, an, b, bn, out, kModeNtt);
+}
+
+int prec_gpu_mul_fft(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
+    return host_mul(a, an, b, bn, out, kModeFft);
+}
+
+int prec_gpu_fft_digit_bits(size_t an, size_t bn) {
+    FftPlan fp;
+    if (an == 0 || bn == 0 || (an > bn ? an : bn) > kFftBandMax || !fft_plan_for(an, bn, fp)) return 0;
+    return fp.b;
 }
 
 int prec_gpu_mul_device(const uint64_t* d_a, size_t an, const uint64_t* d_b, size_t bn, uint64_t* d_out,

@@ -22,7 +22,8 @@ EXPORTS = (
     "prec_gpu_init", "prec_gpu_shutdown", "prec_gpu_mul", "prec_gpu_mul_ntt",
     "prec_gpu_mul_device", "prec_gpu_stream_check", "prec_gpu_last_stats",
     "prec_gpu_ntt_log2", "prec_gpu_strerror", "prec_gpu_mul_device_profile",
-    "prec_gpu_stage_name", "prec_gpu_mul_device_noalloc",
+    "prec_gpu_stage_name", "prec_gpu_mul_device_noalloc", "prec_gpu_mul_fft",
+    "prec_gpu_fft_digit_bits",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -54,7 +55,7 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_init.restype = ctypes.c_int
         L.prec_gpu_shutdown.argtypes = []
         L.prec_gpu_shutdown.restype = None
-        for name in ("prec_gpu_mul", "prec_gpu_mul_ntt"):
+        for name in ("prec_gpu_mul", "prec_gpu_mul_ntt", "prec_gpu_mul_fft"):
             f = getattr(L, name)
             f.argtypes = [_u64p, ctypes.c_size_t, _u64p, ctypes.c_size_t, _u64p]
             f.restype = ctypes.c_int
@@ -65,6 +66,8 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_stream_check.restype = ctypes.c_int
         L.prec_gpu_last_stats.argtypes = [ctypes.POINTER(Stats)]
         L.prec_gpu_last_stats.restype = ctypes.c_int
+        L.prec_gpu_fft_digit_bits.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
+        L.prec_gpu_fft_digit_bits.restype = ctypes.c_int
         L.prec_gpu_ntt_log2.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
         L.prec_gpu_ntt_log2.restype = ctypes.c_int
         L.prec_gpu_mul_device_profile.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
@@ -107,11 +110,12 @@ def init(device: int = -1) -> None:
     check(lib().prec_gpu_init(device), "prec_gpu_init")
 
 
-def mul(a, b, ntt: bool = False) -> np.ndarray:
-    """Product of two host limb vectors (an+bn limbs), computed on the GPU."""
+def mul(a, b, ntt: bool = False, fft: bool = False) -> np.ndarray:
+    """Product of two host limb vectors (an+bn limbs), computed on the GPU:
+    band routing by default, or the NTT / FP64 FFT band forced."""
     a, b = _arr(a), _arr(b)
     out = np.empty(max(len(a) + len(b), 1), dtype=np.uint64)
-    f = lib().prec_gpu_mul_ntt if ntt else lib().prec_gpu_mul
+    f = lib().prec_gpu_mul_ntt if ntt else (lib().prec_gpu_mul_fft if fft else lib().prec_gpu_mul)
     check(f(_p(a), len(a), _p(b), len(b), _p(out)), "prec_gpu_mul")
     return out[: len(a) + len(b)]
 
@@ -140,6 +144,10 @@ def last_stats() -> Stats:
     s = Stats()
     check(lib().prec_gpu_last_stats(ctypes.byref(s)))
     return s
+
+
+def fft_digit_bits(an: int, bn: int) -> int:
+    return lib().prec_gpu_fft_digit_bits(an, bn)
 
 
 def ntt_log2(an: int, bn: int) -> int:

@@ -335,17 +335,130 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+BATCH_COUNT, BATCH_SEED = 4096, 7
+
+
+def run_batch(args):
+    """Batched uneven products: 4096 products, lo log-uniform in [200, 65536]
+    limbs, hi = lo * U[1, 2], SplitMix64 operands.  A step is the whole set.
+    Batched: one H2D of all operands, one graph replay, one D2H of all
+    results.  Plain: prec_gpu_mul per product (host pointers, one call per
+    product).  Both measured end to end, and device-resident."""
+    import torch
+
+    from preclib_gb300 import native, workloads
+    native.init(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    lo, hi = workloads.batch_sizes(BATCH_SEED, BATCH_COUNT)
+    sizes = [(int(h), int(l)) for l, h in zip(lo, hi)]
+    offs, o = [], 0
+    for a, b in sizes:
+        offs.append(o)
+        o += a + b
+    host = workloads.splitmix64(BATCH_SEED, o)
+    host_in = torch.from_numpy(host.view(np.int64)).pin_memory()
+    host_out = torch.empty(o, dtype=torch.int64).pin_memory()
+    d_in = torch.empty(o, dtype=torch.int64, device=dev)
+    d_out = torch.empty(o, dtype=torch.int64, device=dev)
+    bi, bo = d_in.data_ptr(), d_out.data_ptr()
+    items = [(bi + 8 * off, a, bi + 8 * (off + a), b, bo + 8 * off) for off, (a, b) in zip(offs, sizes)]
+    batch = native.Batch(items)
+    ncls, nbytes = batch.info()
+
+    def batched_e2e():
+        d_in.copy_(host_in, non_blocking=True)
+        batch.run(sptr)
+        host_out.copy_(d_out, non_blocking=True)
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        batched_e2e()
+    native.stream_check(sptr)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        batched_e2e()
+    batched_s = (time.perf_counter() - t) / args.steps
+    batched_out = host_out.numpy().view(np.uint64).copy()
+    # device-resident batch (graph replay only)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run(sptr)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    batched_dev_s = e0.elapsed_time(e1) / 1e3 / args.steps
+
+    # plain path: one prec_gpu_mul call per product, host pointers
+    pin = host_in.numpy().view(np.uint64)
+    pout = host_out.numpy().view(np.uint64)
+    L = native.lib()
+    base_i = pin.ctypes.data
+    base_o = pout.ctypes.data
+    u64p = native._u64p
+    calls = [(ctypes_cast(base_i + 8 * off, u64p), a, ctypes_cast(base_i + 8 * (off + a), u64p), b,
+              ctypes_cast(base_o + 8 * off, u64p)) for off, (a, b) in zip(offs, sizes)]
+    plain_steps = max(1, min(args.steps, 3))
+    for c in calls[:64]:
+        native.check(L.prec_gpu_mul(*c))
+    t = time.perf_counter()
+    for _ in range(plain_steps):
+        for c in calls:
+            native.check(L.prec_gpu_mul(*c))
+    plain_s = (time.perf_counter() - t) / plain_steps
+    mismatches = sum(not np.array_equal(batched_out[off:off + a + b], pout[off:off + a + b])
+                     for off, (a, b) in zip(offs, sizes))
+    # plain device-resident: prec_gpu_mul_device per product
+    e0.record(stream)
+    for it in items:
+        native.check(L.prec_gpu_mul_device(*it, sptr or None))
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_dev_s = e0.elapsed_time(e1) / 1e3
+    batch.close()
+    n = BATCH_COUNT
+    line = {
+        "metric": "batched products/s (4096 uneven products)", "value": round(n / batched_s, 1),
+        "unit": "products/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(batched_s * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "4096 products, lo log-uniform [200, 65536] limbs, hi = lo*U[1,2], "
+                               "SplitMix64 seed 7", "limbs_in": o, "length_classes": ncls,
+                   "device_bytes": nbytes, "l2": "inputs (%.0f MB) exceed L2" % (16 * o / 1e6)},
+        "plain_products_per_s": round(n / plain_s, 1),
+        "batched_vs_plain": round(plain_s / batched_s, 2),
+        "device": {"batched_products_per_s": round(n / batched_dev_s, 1),
+                   "plain_products_per_s": round(n / plain_dev_s, 1),
+                   "batched_vs_plain": round(plain_dev_s / batched_dev_s, 2)},
+        "mismatches_vs_plain": int(mismatches),
+        "e2e": {"value": round(n / batched_s, 1), "unit": "products/s", "h2d_bytes_per_step": 8 * o,
+                "d2h_bytes_per_step": 8 * o},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def ctypes_cast(addr, typ):
+    import ctypes
+    return ctypes.cast(ctypes.c_void_p(addr), typ)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="1m", choices=["1m", "batch"],
+                    help="1m: the 1M x 1M product (default line); batch: 4096 uneven products")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -118,6 +118,40 @@ const char *prec_gpu_stage_name(int path, int stage);
 int prec_gpu_mul_device_noalloc(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
                                 uint64_t *d_out, void *stream);
 
+/* ---- batch form: many independent products of uneven sizes -------------
+ * Replaces: nothing one-to-one; the reference forms products one at a time
+ * (operator*, src/mul_basic.cpp:278-284), including the independent
+ * products of one binary-splitting level (pi/pi_chudnovsky.cpp:141-144).
+ * All pointers are device pointers; out receives an+bn limbs. */
+typedef struct prec_gpu_product {
+    const uint64_t *a;
+    size_t an;
+    const uint64_t *b;
+    size_t bn;
+    uint64_t *out;
+} prec_gpu_product_t;
+
+typedef struct prec_gpu_batch prec_gpu_batch_t;
+
+/* Plans a batch: groups the products by transform length (length classes),
+ * allocates their descriptors and workspaces.  No product is computed. */
+int prec_gpu_batch_create(const prec_gpu_product_t *items, size_t count, prec_gpu_batch_t **batch);
+
+/* Computes every product of the batch on `stream` (asynchronous).  The first
+ * call captures the work into a CUDA graph (one stream branch per length
+ * class); later calls replay it, recomputing the products from the current
+ * contents of the same operand buffers. */
+int prec_gpu_batch_run(prec_gpu_batch_t *batch, void *stream);
+
+/* Number of length classes and device bytes the batch holds. */
+int prec_gpu_batch_info(const prec_gpu_batch_t *batch, size_t *classes, size_t *device_bytes);
+
+/* Waits for the device and frees the batch. */
+void prec_gpu_batch_destroy(prec_gpu_batch_t *batch);
+
+/* One-shot batch on `stream`, synchronous (plan, run without a graph, free). */
+int prec_gpu_mul_batch(const prec_gpu_product_t *items, size_t count, void *stream);
+
 /* Synchronises `stream` and reports any device-side error raised by work
  * the library enqueued (PREC_GPU_E_TIMEOUT, PREC_GPU_E_INTERNAL) or a
  * CUDA error. */

@@ -20,10 +20,12 @@ constexpr int kBlockLimbs = kCarryThreads * kCarryLimbs;
 // scratch layout: [0] finished-block counter, [1 .. nblk] aggregates
 // (bit0 G, bit1 P)
 template <int SET>
-__global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args) {
+__global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     __shared__ BlockCarryShared sh;
     __shared__ uint32_t s_last;
+    select_product(args, batch);
     const uint32_t bid = blockIdx.x;
+    if ((int)bid >= args.nblk) return;  // batch: a shorter product of the class
     const uint64_t N = 1ull << args.k;
     const uint32_t* __restrict__ r0 = args.work;
     const uint32_t* __restrict__ r1 = args.work + 2 * N;
@@ -88,11 +90,11 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args) {
     // ---- phase 2: the last block resolves the carries between blocks
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&args.scratch[0], 1u) == gridDim.x - 1 ? 1u : 0u;
+    if (threadIdx.x == 0) s_last = atomicAdd(&args.scratch[0], 1u) == (uint32_t)args.nblk - 1 ? 1u : 0u;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    const int nblk = gridDim.x;
+    const int nblk = args.nblk;
     const int per = (nblk + blockDim.x - 1) / blockDim.x;  // aggregates per thread
     const int b0 = threadIdx.x * per;
     // this thread's run of blocks as one carry element
@@ -121,9 +123,18 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args) {
     if (b0 < nblk && b0 + per >= nblk && c) atomicOr(args.err, kDevErrCarry);
 }
 
-void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st) {
-    if (set == 0) k_crt_carry<0><<<a.nblk, kCarryThreads, 0, st>>>(a);
-    else k_crt_carry<1><<<a.nblk, kCarryThreads, 0, st>>>(a);
+void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int max_nblk) {
+    const dim3 grid(batch ? max_nblk : a.nblk, 1, count);
+    if (set == 0) k_crt_carry<0><<<grid, kCarryThreads, 0, st>>>(a, batch);
+    else k_crt_carry<1><<<grid, kCarryThreads, 0, st>>>(a, batch);
+}
+
+void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch, int count, int max_nblk,
+                            cudaStream_t st) {
+    launch_fwd_cols(set, args, st, batch, count);
+    launch_rows(set, args, st, batch, count);
+    launch_inv_cols(set, args, st, batch, count);
+    launch_crt_carry(set, args, st, batch, count, max_nblk);
 }
 
 void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev) {

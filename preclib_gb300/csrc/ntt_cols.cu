@@ -16,10 +16,11 @@
 namespace precgpu {
 
 template <int SET, int M, int C>
-__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args) {
+__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
+    select_product(args, batch);
     const int prime = blockIdx.y >> 1, operand = blockIdx.y & 1;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.tf[prime];
@@ -84,10 +85,11 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args)
 }
 
 template <int SET, int M, int C>
-__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args) {
+__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
+    select_product(args, batch);
     const int prime = blockIdx.y;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.ti[prime];
@@ -138,22 +140,22 @@ static size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * siz
 #define PREC_COLS_SET0(X) X(0, 6, 8) X(0, 7, 8) X(0, 8, 8) X(0, 9, 8) X(0, 10, 8) X(0, 11, 8)
 #define PREC_COLS_SET1(X) X(1, 11, 8) X(1, 12, 4) X(1, 13, 4)
 
-void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st) {
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
     const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, 2 * kPrimes);
+    const dim3 grid((1u << a.k2) / cg, 2 * kPrimes, count);
     const size_t smem = col_smem(m, cg);
 #define X(S, MM, CC) \
-    if (set == S && m == MM) { k_fwd_cols<S, MM, CC><<<grid, 256, smem, st>>>(a); return; }
+    if (set == S && m == MM) { k_fwd_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }
     PREC_COLS_SET0(X) PREC_COLS_SET1(X)
 #undef X
 }
 
-void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st) {
+void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
     const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, kPrimes);
+    const dim3 grid((1u << a.k2) / cg, kPrimes, count);
     const size_t smem = col_smem(m, cg);
 #define X(S, MM, CC) \
-    if (set == S && m == MM) { k_inv_cols<S, MM, CC><<<grid, 256, smem, st>>>(a); return; }
+    if (set == S && m == MM) { k_inv_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }
     PREC_COLS_SET0(X) PREC_COLS_SET1(X)
 #undef X
 }

@@ -44,6 +44,39 @@ struct ProdArgs {
     FieldArgs f;
 };
 
+// Per-product part of ProdArgs in the batch form: a length class shares
+// k, k1, k2, rows, crt and f; each product (blockIdx.z) has its own
+// operands, output, work buffer and carry words.
+struct ProdPtrs {
+    const uint64_t* a;
+    const uint64_t* b;
+    uint64_t* out;
+    uint32_t* work;
+    uint32_t* scratch;
+    uint64_t la, lb, lout;
+    int nblk;
+    int pad;
+};
+
+#ifdef __CUDACC__
+// the product this CTA works on: the launch's own arguments, or entry
+// blockIdx.z of a batch's descriptor array
+__device__ __forceinline__ void select_product(ProdArgs& args, const ProdPtrs* __restrict__ batch) {
+    if (batch) {
+        const ProdPtrs& p = batch[blockIdx.z];
+        args.a = p.a;
+        args.b = p.b;
+        args.out = p.out;
+        args.work = p.work;
+        args.scratch = p.scratch;
+        args.la = p.la;
+        args.lb = p.lb;
+        args.lout = p.lout;
+        args.nblk = p.nblk;
+    }
+}
+#endif
+
 // One product of the single-CTA path (transforms up to 2^12 points; also
 // the batch form's small length classes).  Always prime set 0.
 struct SmallDesc {
@@ -73,14 +106,20 @@ int ntt_small_threads(int k);
 void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k,
                       const FieldArgs& f, cudaStream_t st, cudaEvent_t* ev = nullptr);
 void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev = nullptr);
+// the batch form: `count` products of one length class (class-wide fields
+// from `args`, per-product fields from the device array `batch`);
+// max_nblk = the largest carry grid of the class
+void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch, int count, int max_nblk,
+                            cudaStream_t st);
 int ntt_row_threads(int k2, int n1, int* rows);
 int ntt_configure_kernels();  // opt-in shared-memory sizes; returns a cudaError_t
 
 // launchers of each translation unit (ntt_cols.cu, ntt_rows.cu, ntt_carry.cu, ntt_small.cu)
-void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st);
-void launch_rows(int set, const ProdArgs& a, cudaStream_t st);
-void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st);
-void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st);
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1);
+void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1);
+void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1);
+void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
+                      int max_nblk = 0);
 int configure_cols();
 int configure_rows();
 int configure_small();

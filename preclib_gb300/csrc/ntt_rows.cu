@@ -12,11 +12,12 @@
 namespace precgpu {
 
 template <int SET, int M>
-__global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args) {
+__global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "row transforms have at least two passes");
     constexpr int AS = astride_for(M);
+    select_product(args, batch);
     const int prime = blockIdx.y;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ twf = args.f.tf[prime];
@@ -119,13 +120,13 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
 
 #define PREC_ROWS(X) X(0, 7) X(0, 8) X(0, 9) X(0, 10) X(0, 11) X(0, 12) X(1, 13)
 
-void launch_rows(int set, const ProdArgs& a, cudaStream_t st) {
+void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
     const int m = a.k2;
-    const dim3 grid((1u << a.k1) / a.rows, kPrimes);
+    const dim3 grid((1u << a.k1) / a.rows, kPrimes, count);
     const int threads = a.rows << (m - 5);
     const size_t smem = row_smem(m, a.rows);
 #define X(S, MM) \
-    if (set == S && m == MM) { k_rows<S, MM><<<grid, threads, smem, st>>>(a); return; }
+    if (set == S && m == MM) { k_rows<S, MM><<<grid, threads, smem, st>>>(a, batch); return; }
     PREC_ROWS(X)
 #undef X
 }

@@ -1,0 +1,285 @@
+// prec_gpu_batch.cu -- the batch form: many products of uneven sizes.
+//
+// The reference multiplies one pair per call (precn_t operator*,
+// src/mul_basic.cpp:278-284); its only producer of many independent products
+// is binary splitting (pi/pi_chudnovsky.cpp:141-144), one tree level at a
+// time.  Here a batch of device-resident products is planned once:
+//   * every product gets its transform length 2^k (the same plan as a single
+//     product), and products of one length form a length class;
+//   * classes up to 2^12 points run one single-CTA product per CTA in one
+//     launch; larger classes run the four-step kernels once per pass over
+//     all their products (grid.z = product, per-product pointers in a
+//     device descriptor array), in chunks bounded by a workspace budget;
+//   * each class gets its own stream branch, so classes overlap on the GPU;
+//   * the first prec_gpu_batch_run captures all of it into one CUDA graph
+//     (descriptors and workspaces have fixed addresses), later runs replay
+//     the graph with a single launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/prec_gpu.h"
+#include "prec_gpu_internal.h"
+
+using namespace precgpu;
+
+namespace {
+
+struct Chunk {
+    int first = 0, count = 0;  // entries of the class's descriptor array
+    int max_nblk = 0;
+};
+
+struct Cls {
+    int k = 0;
+    Plan pl;                      // class-wide plan (k, set, k1, k2, rows, crt)
+    std::vector<int> items;       // indices into the batch's products
+    size_t ws_per = 0;            // workspace bytes per product (four-step)
+    int per_chunk = 0;            // products per chunk
+    std::vector<Chunk> chunks;
+    SmallDesc* d_small = nullptr; // device descriptors (single-CTA classes)
+    ProdPtrs* d_ptrs = nullptr;   // device descriptors (four-step classes)
+    uint8_t* ws = nullptr;        // workspace of one chunk
+    cudaStream_t stream = nullptr;
+    cudaEvent_t join = nullptr;
+};
+
+size_t env_bytes(const char* name, size_t dflt) {
+    const char* s = std::getenv(name);
+    if (!s) return dflt;
+    const double v = std::atof(s);
+    return v > 0 ? (size_t)v : dflt;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct prec_gpu_batch {
+    std::vector<prec_gpu_product_t> items;
+    std::vector<Cls> classes;
+    std::vector<int> zero_items;  // products with a zero-length operand
+    void* d_mem = nullptr;
+    size_t d_bytes = 0;
+    cudaStream_t cap = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int* err = nullptr;
+};
+
+static void batch_free(prec_gpu_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (Cls& c : b->classes) {
+        if (c.stream) cudaStreamDestroy(c.stream);
+        if (c.join) cudaEventDestroy(c.join);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->d_mem) cudaFree(b->d_mem);
+    delete b;
+}
+
+#define BCK(x)                                  \
+    do {                                        \
+        cudaError_t _e = (x);                   \
+        if (_e != cudaSuccess) {                \
+            batch_free(b);                      \
+            return cuda_code(_e);               \
+        }                                       \
+    } while (0)
+
+// all of the batch's device work, enqueued on the class streams (forked
+// from and joined to `origin`), or on `origin` alone when `branch` is false
+static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
+    if (branch) cudaEventRecord(b->fork, origin);
+    for (int i : b->zero_items) {
+        const prec_gpu_product_t& p = b->items[i];
+        if (p.an + p.bn) cudaMemsetAsync(p.out, 0, (p.an + p.bn) * sizeof(uint64_t), origin);
+    }
+    for (Cls& c : b->classes) {
+        cudaStream_t st = branch ? c.stream : origin;
+        if (branch) cudaStreamWaitEvent(st, b->fork, 0);
+        if (c.pl.path == 0) {
+            ntt_launch_small(c.d_small, nullptr, (int)c.items.size(), c.k, ctx_field(0), st);
+        } else {
+            ProdArgs args{};
+            args.err = b->err;
+            args.k = c.pl.k;
+            args.k1 = c.pl.k1;
+            args.k2 = c.pl.k2;
+            args.rows = c.pl.rows;
+            args.crt = c.pl.crt;
+            args.f = ctx_field(c.pl.set);
+            for (const Chunk& ch : c.chunks)
+                ntt_launch_4step_batch(c.pl.set, args, c.d_ptrs + ch.first, ch.count, ch.max_nblk, st);
+        }
+        if (branch) {
+            cudaEventRecord(c.join, st);
+            cudaStreamWaitEvent(origin, c.join, 0);
+        }
+    }
+}
+
+extern "C" {
+
+int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gpu_batch_t** out) {
+    if (!out || (!items && count)) return PREC_GPU_E_ARG;
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx_mutex());
+    int r = ctx_init_locked(-1);
+    if (r) return r;
+    prec_gpu_batch* b = new prec_gpu_batch();
+    b->items.assign(items, items + count);
+    b->err = ctx_device_err();
+    std::map<int, Cls> by_k;
+    for (size_t i = 0; i < count; ++i) {
+        const prec_gpu_product_t& p = items[i];
+        if ((p.an && !p.a) || (p.bn && !p.b) || (p.an + p.bn && !p.out)) {
+            batch_free(b);
+            return PREC_GPU_E_ARG;
+        }
+        if (p.an == 0 || p.bn == 0) {
+            b->zero_items.push_back((int)i);
+            continue;
+        }
+        Plan pl;
+        if ((r = plan_for(2 * (uint64_t)p.an, 2 * (uint64_t)p.bn, p.an + p.bn, pl))) {
+            batch_free(b);
+            return r;
+        }
+        Cls& c = by_k[pl.k];
+        if (c.items.empty()) {
+            c.k = pl.k;
+            c.pl = pl;
+        }
+        c.items.push_back((int)i);
+    }
+    // device layout: descriptors, then one workspace per four-step class
+    const size_t budget = env_bytes("PREC_GPU_BATCH_CLASS_BYTES", (size_t)1 << 30);
+    size_t bytes = 0;
+    std::vector<size_t> desc_off, ws_off;
+    for (auto& kv : by_k) {
+        Cls& c = kv.second;
+        const size_t n = c.items.size();
+        desc_off.push_back(bytes);
+        bytes += align256(n * (c.pl.path == 0 ? sizeof(SmallDesc) : sizeof(ProdPtrs)));
+        if (c.pl.path == 1) {
+            const size_t carry_words = (size_t)(((1ull << c.k) / 2) / (kCarryThreads * kCarryLimbs)) + 2;
+            c.ws_per = align256(((size_t)2 * kPrimes << c.k) * sizeof(uint32_t) + carry_words * sizeof(uint32_t));
+            c.per_chunk = (int)std::min<size_t>({n, std::max<size_t>(1, budget / c.ws_per), 65535});
+            ws_off.push_back(bytes);
+            bytes += c.ws_per * c.per_chunk;
+        } else {
+            ws_off.push_back(0);
+        }
+        b->classes.push_back(c);
+    }
+    b->d_bytes = bytes;
+    if (bytes) BCK(cudaMalloc(&b->d_mem, bytes));
+    uint8_t* base = static_cast<uint8_t*>(b->d_mem);
+    for (size_t ci = 0; ci < b->classes.size(); ++ci) {
+        Cls& c = b->classes[ci];
+        const size_t n = c.items.size();
+        if (c.pl.path == 0) {
+            std::vector<SmallDesc> h(n);
+            for (size_t j = 0; j < n; ++j) {
+                const prec_gpu_product_t& p = items[c.items[j]];
+                SmallDesc& d = h[j];
+                d.a = p.a;
+                d.b = p.b;
+                d.out = p.out;
+                d.la = p.an;
+                d.lb = p.bn;
+                d.lout = p.an + p.bn;
+                d.k = c.k;
+                d.pad = 0;
+                d.crt = c.pl.crt;
+            }
+            c.d_small = reinterpret_cast<SmallDesc*>(base + desc_off[ci]);
+            BCK(cudaMemcpy(c.d_small, h.data(), n * sizeof(SmallDesc), cudaMemcpyHostToDevice));
+        } else {
+            c.ws = base + ws_off[ci];
+            std::vector<ProdPtrs> h(n);
+            const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+            for (size_t j = 0; j < n; ++j) {
+                const prec_gpu_product_t& p = items[c.items[j]];
+                ProdPtrs& d = h[j];
+                uint8_t* w = c.ws + c.ws_per * (j % c.per_chunk);  // chunks reuse the workspace
+                d.a = p.a;
+                d.b = p.b;
+                d.out = p.out;
+                d.work = reinterpret_cast<uint32_t*>(w);
+                d.scratch = d.work + ((size_t)2 * kPrimes << c.k);
+                d.la = p.an;
+                d.lb = p.bn;
+                d.lout = p.an + p.bn;
+                d.nblk = (int)((d.lout + bl - 1) / bl);
+                d.pad = 0;
+            }
+            for (size_t f = 0; f < n; f += c.per_chunk) {
+                Chunk ch;
+                ch.first = (int)f;
+                ch.count = (int)std::min<size_t>(c.per_chunk, n - f);
+                for (int j = 0; j < ch.count; ++j) ch.max_nblk = std::max(ch.max_nblk, h[f + j].nblk);
+                c.chunks.push_back(ch);
+            }
+            c.d_ptrs = reinterpret_cast<ProdPtrs*>(base + desc_off[ci]);
+            BCK(cudaMemcpy(c.d_ptrs, h.data(), n * sizeof(ProdPtrs), cudaMemcpyHostToDevice));
+        }
+        BCK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        BCK(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
+    }
+    BCK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+    BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    *out = b;
+    return PREC_GPU_OK;
+}
+
+int prec_gpu_batch_run(prec_gpu_batch_t* b, void* stream) {
+    if (!b) return PREC_GPU_E_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!b->exec) {
+        cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_code(e);
+        batch_enqueue(b, b->cap, true);
+        e = cudaStreamEndCapture(b->cap, &b->graph);
+        if (e != cudaSuccess) return cuda_code(e);
+        e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) return cuda_code(e);
+    }
+    return cuda_code(cudaGraphLaunch(b->exec, st));
+}
+
+int prec_gpu_batch_info(const prec_gpu_batch_t* b, size_t* classes, size_t* device_bytes) {
+    if (!b) return PREC_GPU_E_ARG;
+    if (classes) *classes = b->classes.size();
+    if (device_bytes) *device_bytes = b->d_bytes;
+    return PREC_GPU_OK;
+}
+
+void prec_gpu_batch_destroy(prec_gpu_batch_t* b) {
+    if (b) cudaDeviceSynchronize();
+    batch_free(b);
+}
+
+int prec_gpu_mul_batch(const prec_gpu_product_t* items, size_t count, void* stream) {
+    prec_gpu_batch_t* b = nullptr;
+    int r = prec_gpu_batch_create(items, count, &b);
+    if (r) return r;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    batch_enqueue(b, st, false);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    batch_free(b);
+    return cuda_code(e);
+}
+
+}  // extern "C"

@@ -21,6 +21,7 @@
 #include "../../include/prec_gpu.h"
 #include "fft_kernels.cuh"
 #include "ntt_kernels.cuh"
+#include "prec_gpu_internal.h"
 
 namespace precgpu {
 
@@ -75,16 +76,6 @@ constexpr size_t kStatBytes = 16;       // device status block (error bits, FFT 
 constexpr size_t kFftBandMin = 192;     // src/mul_basic.cpp:4 (FFT above 192 limbs)
 constexpr size_t kFftBandMax = 6144;    // src/mul_basic.cpp:5 (NTT above 6144 limbs)
 
-struct Plan {
-    int k = 0, k1 = 0, k2 = 0;
-    int set = 0;
-    int path = 0;  // 0 single CTA, 1 four-step
-    int nblk = 0;
-    int rows = 0;  // rows per CTA of the row pass
-    CrtConst crt{};
-    size_t work_bytes = 0;
-};
-
 static CrtConst crt_for(int set, int k) {
     const uint32_t* P = kP[set];
     const uint32_t p1 = P[0], p2 = P[1], p3 = P[2];
@@ -107,7 +98,7 @@ static CrtConst crt_for(int set, int k) {
 }
 
 // da, db: 32-bit digit counts (upper bounds are fine)
-static int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
+int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
     const uint64_t need = da + db - 1;
     int k = kSmallMinLog2;
     while ((1ull << k) < need) ++k;
@@ -155,7 +146,7 @@ struct Ctx {
 static Ctx g_ctx;
 static thread_local prec_gpu_stats_t t_stats;
 
-static int cuda_code(cudaError_t e) {
+int cuda_code(cudaError_t e) {
     if (e == cudaSuccess) return 0;
     if (e == cudaErrorMemoryAllocation) return PREC_GPU_E_NOMEM;
     if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return PREC_GPU_E_NODEV;
@@ -262,6 +253,11 @@ static int init_locked(Ctx& c, int device) {
     c.ready = true;
     return 0;
 }
+
+std::mutex& ctx_mutex() { return g_ctx.mu; }
+int ctx_init_locked(int device) { return init_locked(g_ctx, device); }
+const FieldArgs& ctx_field(int set) { return g_ctx.field[set]; }
+int* ctx_device_err() { return g_ctx.d_err; }
 
 static int ensure_ws(Ctx& c, size_t bytes) {
     if (bytes <= c.ws_cap) return 0;

@@ -23,7 +23,8 @@ EXPORTS = (
     "prec_gpu_mul_device", "prec_gpu_stream_check", "prec_gpu_last_stats",
     "prec_gpu_ntt_log2", "prec_gpu_strerror", "prec_gpu_mul_device_profile",
     "prec_gpu_stage_name", "prec_gpu_mul_device_noalloc", "prec_gpu_mul_fft",
-    "prec_gpu_fft_digit_bits",
+    "prec_gpu_fft_digit_bits", "prec_gpu_batch_create", "prec_gpu_batch_run", "prec_gpu_batch_info",
+    "prec_gpu_batch_destroy", "prec_gpu_mul_batch",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -33,6 +34,12 @@ class Stats(ctypes.Structure):
     _fields_ = [("path", ctypes.c_int), ("log2_n", ctypes.c_int),
                 ("limbs_a", ctypes.c_size_t), ("limbs_b", ctypes.c_size_t),
                 ("fft_max_distance", ctypes.c_double), ("device_ms", ctypes.c_double)]
+
+
+class Product(ctypes.Structure):
+    """prec_gpu_product_t: device pointers and limb counts of one product."""
+    _fields_ = [("a", ctypes.c_void_p), ("an", ctypes.c_size_t), ("b", ctypes.c_void_p),
+                ("bn", ctypes.c_size_t), ("out", ctypes.c_void_p)]
 
 
 class PrecGpuError(RuntimeError):
@@ -78,6 +85,18 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_mul_device_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                                   ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         L.prec_gpu_mul_device_noalloc.restype = ctypes.c_int
+        L.prec_gpu_batch_create.argtypes = [ctypes.POINTER(Product), ctypes.c_size_t,
+                                            ctypes.POINTER(ctypes.c_void_p)]
+        L.prec_gpu_batch_create.restype = ctypes.c_int
+        L.prec_gpu_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.prec_gpu_batch_run.restype = ctypes.c_int
+        L.prec_gpu_batch_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
+                                          ctypes.POINTER(ctypes.c_size_t)]
+        L.prec_gpu_batch_info.restype = ctypes.c_int
+        L.prec_gpu_batch_destroy.argtypes = [ctypes.c_void_p]
+        L.prec_gpu_batch_destroy.restype = None
+        L.prec_gpu_mul_batch.argtypes = [ctypes.POINTER(Product), ctypes.c_size_t, ctypes.c_void_p]
+        L.prec_gpu_mul_batch.restype = ctypes.c_int
         L.prec_gpu_stage_name.argtypes = [ctypes.c_int, ctypes.c_int]
         L.prec_gpu_stage_name.restype = ctypes.c_char_p
         L.prec_gpu_strerror.argtypes = [ctypes.c_int]
@@ -152,3 +171,39 @@ def fft_digit_bits(an: int, bn: int) -> int:
 
 def ntt_log2(an: int, bn: int) -> int:
     return lib().prec_gpu_ntt_log2(an, bn)
+
+
+class Batch:
+    """A planned batch of device-resident products (prec_gpu_batch_t).
+
+    items: sequence of (a_ptr, an, b_ptr, bn, out_ptr) device pointers."""
+
+    def __init__(self, items):
+        arr = (Product * max(len(items), 1))(*[Product(*it) for it in items])
+        self._h = ctypes.c_void_p()
+        check(lib().prec_gpu_batch_create(arr, len(items), ctypes.byref(self._h)), "prec_gpu_batch_create")
+
+    def run(self, stream: int = 0) -> None:
+        check(lib().prec_gpu_batch_run(self._h, stream or None), "prec_gpu_batch_run")
+
+    def info(self):
+        c, b = ctypes.c_size_t(), ctypes.c_size_t()
+        check(lib().prec_gpu_batch_info(self._h, ctypes.byref(c), ctypes.byref(b)))
+        return c.value, b.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().prec_gpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mul_batch(items, stream: int = 0) -> None:
+    """One-shot batch (synchronous) of (a_ptr, an, b_ptr, bn, out_ptr) products."""
+    arr = (Product * max(len(items), 1))(*[Product(*it) for it in items])
+    check(lib().prec_gpu_mul_batch(arr, len(items), stream or None), "prec_gpu_mul_batch")

@@ -439,6 +439,102 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+SERVE_SEED = 11
+
+
+def run_serve(args):
+    """Serving loop: requests with device-resident operands (slices of one
+    random device buffer), an = bn = s with s log-uniform in [256, 4194304]
+    limbs.  Capacity = products/s with every request queued at once; then
+    Poisson arrivals at 10..90 % of capacity, p50/p99 latency per load.
+    A sample of results is recomputed alone and compared with the mix."""
+    import hashlib
+
+    import torch
+
+    from preclib_gb300 import native, workloads
+    native.init(0)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(SERVE_SEED)
+    n_cap, n_load = 400, 300
+    pool_limbs = 1 << 23
+    d_pool = torch.from_numpy(workloads.splitmix64(SERVE_SEED, pool_limbs).view(np.int64)).to(dev)
+    base = d_pool.data_ptr()
+
+    def make(n):
+        s = np.rint(np.exp(rng.uniform(np.log(256), np.log(4194304), n))).astype(np.int64)
+        reqs, tot = [], 0
+        for x in s:
+            x = int(x)
+            oa = int(rng.integers(0, pool_limbs - x + 1))
+            ob = int(rng.integers(0, pool_limbs - x + 1))
+            reqs.append((base + 8 * oa, x, base + 8 * ob, x, tot))
+            tot += 2 * x
+        return reqs, tot
+
+    budget = 24 << 30
+    srv = native.Server(budget, slots=16)
+
+    def run_set(reqs, out, rate):
+        ob = out.data_ptr()
+        tickets = []
+        t0 = time.perf_counter()
+        t_next = t0
+        for (a, an, b, bn, off) in reqs:
+            if rate:
+                t_next += rng.exponential(1.0 / rate)
+                while time.perf_counter() < t_next:
+                    pass
+            tickets.append(srv.submit(a, an, b, bn, ob + 8 * off))
+        srv.drain(600)
+        lat = np.array([srv.wait(t, 1.0) for t in tickets])
+        span = time.perf_counter() - t0
+        return lat, len(reqs) / span
+
+    # warm-up, then capacity (all queued at once)
+    reqs, tot = make(64)
+    out = torch.empty(tot, dtype=torch.int64, device=dev)
+    run_set(reqs, out, 0)
+    reqs, tot = make(n_cap)
+    out = torch.empty(tot, dtype=torch.int64, device=dev)
+    lat, capacity = run_set(reqs, out, 0)
+    # alone vs mixed on a sample of the capacity run
+    mismatches = 0
+    for (a, an, b, bn, off) in reqs[::20]:
+        alone = torch.empty(an + bn, dtype=torch.int64, device=dev)
+        native.mul_device(a, an, b, bn, alone.data_ptr())
+        native.stream_check()
+        h1 = hashlib.sha256(alone.cpu().numpy().tobytes()).hexdigest()
+        h2 = hashlib.sha256(out[off:off + an + bn].cpu().numpy().tobytes()).hexdigest()
+        mismatches += h1 != h2
+    del out
+    loads = []
+    for load in (0.1, 0.3, 0.5, 0.7, 0.9):
+        reqs, tot = make(n_load)
+        out = torch.empty(tot, dtype=torch.int64, device=dev)
+        lat, rate = run_set(reqs, out, load * capacity)
+        loads.append({"load": load, "offered_per_s": round(load * capacity, 1), "products_per_s": round(rate, 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)), 3)})
+        del out
+    st = srv.stats()
+    srv.close()
+    mid = [x for x in loads if x["load"] == 0.5][0]
+    line = {
+        "metric": "serving p99 latency ms at 50% load (Poisson arrivals)", "value": mid["p99_ms"], "unit": "ms",
+        "n_gpus": 1, "steps": len(loads), "warmup": 1, "ms_per_step": None, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "an = bn = s, s log-uniform [256, 4194304] limbs, device-resident operands, "
+                               "SplitMix64 seed 11", "hbm_budget_bytes": budget, "slots": 16,
+                   "requests_capacity_run": n_cap, "requests_per_load": n_load},
+        "capacity_products_per_s": round(capacity, 1),
+        "loads": loads,
+        "peak_in_flight": st.peak_in_flight, "peak_workspace_bytes": st.peak_bytes,
+        "mismatches_alone_vs_mixed": int(mismatches), "checked": len(range(0, n_cap, 20)),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_cast(addr, typ):
     import ctypes
     return ctypes.cast(ctypes.c_void_p(addr), typ)
@@ -450,8 +546,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="1m", choices=["1m", "batch"],
-                    help="1m: the 1M x 1M product (default line); batch: 4096 uneven products")
+    ap.add_argument("--workload", default="1m", choices=["1m", "batch", "serve"],
+                    help="1m: the 1M x 1M product (default line); batch: 4096 uneven products; "
+                         "serve: serving loop under Poisson arrivals")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
@@ -459,6 +556,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

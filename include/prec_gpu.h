@@ -152,6 +152,42 @@ void prec_gpu_batch_destroy(prec_gpu_batch_t *batch);
 /* One-shot batch on `stream`, synchronous (plan, run without a graph, free). */
 int prec_gpu_mul_batch(const prec_gpu_product_t *items, size_t count, void *stream);
 
+/* ---- serving loop: continuous admission of requests ---------------------
+ * Replaces: nothing in the reference (single-threaded, one product per
+ * call).  A server owns `slots` CUDA streams, a private memory pool and a
+ * worker thread.  Requests (device-resident operands and output) are
+ * admitted while a slot is free and the transform workspace fits
+ * `hbm_budget_bytes`; admitted requests run concurrently on their own
+ * streams.  Latency = host time from submit to observed completion. */
+typedef struct prec_gpu_server prec_gpu_server_t;
+
+typedef struct prec_gpu_serve_stats {
+    uint64_t submitted, completed, failed;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* latency of completed requests */
+    double products_per_s;                   /* completed / (last completion - first submit) */
+    size_t peak_bytes;                       /* largest admitted workspace total */
+    int peak_in_flight;                      /* most requests on the GPU at once */
+} prec_gpu_serve_stats_t;
+
+int prec_gpu_serve_create(size_t hbm_budget_bytes, int slots, prec_gpu_server_t **server);
+
+/* Queues one product; returns at once with its ticket.  PREC_GPU_E_NOMEM if
+ * its workspace alone exceeds the budget. */
+int prec_gpu_serve_submit(prec_gpu_server_t *server, const uint64_t *d_a, size_t an, const uint64_t *d_b,
+                          size_t bn, uint64_t *d_out, uint64_t *ticket);
+
+/* Waits (host side, at most timeout_s) for one ticket; returns its status
+ * and latency, or PREC_GPU_E_TIMEOUT. */
+int prec_gpu_serve_wait(prec_gpu_server_t *server, uint64_t ticket, double timeout_s, double *latency_ms);
+
+/* Waits (host side, at most timeout_s) until every submitted request completed. */
+int prec_gpu_serve_drain(prec_gpu_server_t *server, double timeout_s);
+
+int prec_gpu_serve_stats(prec_gpu_server_t *server, prec_gpu_serve_stats_t *stats);
+
+/* Finishes the queued work, stops the worker and frees the server. */
+void prec_gpu_serve_destroy(prec_gpu_server_t *server);
+
 /* Synchronises `stream` and reports any device-side error raised by work
  * the library enqueued (PREC_GPU_E_TIMEOUT, PREC_GPU_E_INTERNAL) or a
  * CUDA error. */

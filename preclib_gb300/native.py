@@ -24,7 +24,8 @@ EXPORTS = (
     "prec_gpu_ntt_log2", "prec_gpu_strerror", "prec_gpu_mul_device_profile",
     "prec_gpu_stage_name", "prec_gpu_mul_device_noalloc", "prec_gpu_mul_fft",
     "prec_gpu_fft_digit_bits", "prec_gpu_batch_create", "prec_gpu_batch_run", "prec_gpu_batch_info",
-    "prec_gpu_batch_destroy", "prec_gpu_mul_batch",
+    "prec_gpu_batch_destroy", "prec_gpu_mul_batch", "prec_gpu_serve_create", "prec_gpu_serve_submit",
+    "prec_gpu_serve_wait", "prec_gpu_serve_drain", "prec_gpu_serve_stats", "prec_gpu_serve_destroy",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -40,6 +41,13 @@ class Product(ctypes.Structure):
     """prec_gpu_product_t: device pointers and limb counts of one product."""
     _fields_ = [("a", ctypes.c_void_p), ("an", ctypes.c_size_t), ("b", ctypes.c_void_p),
                 ("bn", ctypes.c_size_t), ("out", ctypes.c_void_p)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("products_per_s", ctypes.c_double),
+                ("peak_bytes", ctypes.c_size_t), ("peak_in_flight", ctypes.c_int)]
 
 
 class PrecGpuError(RuntimeError):
@@ -97,6 +105,20 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_batch_destroy.restype = None
         L.prec_gpu_mul_batch.argtypes = [ctypes.POINTER(Product), ctypes.c_size_t, ctypes.c_void_p]
         L.prec_gpu_mul_batch.restype = ctypes.c_int
+        L.prec_gpu_serve_create.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        L.prec_gpu_serve_create.restype = ctypes.c_int
+        L.prec_gpu_serve_submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                            ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+        L.prec_gpu_serve_submit.restype = ctypes.c_int
+        L.prec_gpu_serve_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double,
+                                          ctypes.POINTER(ctypes.c_double)]
+        L.prec_gpu_serve_wait.restype = ctypes.c_int
+        L.prec_gpu_serve_drain.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.prec_gpu_serve_drain.restype = ctypes.c_int
+        L.prec_gpu_serve_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServeStats)]
+        L.prec_gpu_serve_stats.restype = ctypes.c_int
+        L.prec_gpu_serve_destroy.argtypes = [ctypes.c_void_p]
+        L.prec_gpu_serve_destroy.restype = None
         L.prec_gpu_stage_name.argtypes = [ctypes.c_int, ctypes.c_int]
         L.prec_gpu_stage_name.restype = ctypes.c_char_p
         L.prec_gpu_strerror.argtypes = [ctypes.c_int]
@@ -207,3 +229,42 @@ def mul_batch(items, stream: int = 0) -> None:
     """One-shot batch (synchronous) of (a_ptr, an, b_ptr, bn, out_ptr) products."""
     arr = (Product * max(len(items), 1))(*[Product(*it) for it in items])
     check(lib().prec_gpu_mul_batch(arr, len(items), stream or None), "prec_gpu_mul_batch")
+
+
+class Server:
+    """Serving loop (prec_gpu_server_t): device-resident requests admitted by
+    HBM footprint into `slots` concurrent streams."""
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 8):
+        self._h = ctypes.c_void_p()
+        check(lib().prec_gpu_serve_create(hbm_budget_bytes, slots, ctypes.byref(self._h)), "prec_gpu_serve_create")
+
+    def submit(self, a_ptr: int, an: int, b_ptr: int, bn: int, out_ptr: int) -> int:
+        t = ctypes.c_uint64()
+        check(lib().prec_gpu_serve_submit(self._h, a_ptr, an, b_ptr, bn, out_ptr, ctypes.byref(t)),
+              "prec_gpu_serve_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> float:
+        ms = ctypes.c_double()
+        check(lib().prec_gpu_serve_wait(self._h, ticket, timeout_s, ctypes.byref(ms)), "prec_gpu_serve_wait")
+        return ms.value
+
+    def drain(self, timeout_s: float = 300.0) -> None:
+        check(lib().prec_gpu_serve_drain(self._h, timeout_s), "prec_gpu_serve_drain")
+
+    def stats(self) -> ServeStats:
+        st = ServeStats()
+        check(lib().prec_gpu_serve_stats(self._h, ctypes.byref(st)))
+        return st
+
+    def close(self) -> None:
+        if self._h:
+            lib().prec_gpu_serve_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -23,13 +23,13 @@ template <int SET>
 __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     __shared__ BlockCarryShared sh;
     __shared__ uint32_t s_last;
-    select_product(args, batch);
+    const ProdPtrs PP = select_product(args, batch);
     const uint32_t bid = blockIdx.x;
-    if ((int)bid >= args.nblk) return;  // batch: a shorter product of the class
+    if ((int)bid >= PP.nblk) return;  // batch: a shorter product of the class
     const uint64_t N = 1ull << args.k;
-    const uint32_t* __restrict__ r0 = args.work;
-    const uint32_t* __restrict__ r1 = args.work + 2 * N;
-    const uint32_t* __restrict__ r2 = args.work + 4 * N;
+    const uint32_t* __restrict__ r0 = PP.work;
+    const uint32_t* __restrict__ r1 = PP.work + 2 * N;
+    const uint32_t* __restrict__ r2 = PP.work + 4 * N;
     const int lane = threadIdx.x & 31;
     const int64_t m0 = (int64_t)bid * kBlockLimbs + threadIdx.x * kCarryLimbs;
     const uint64_t i0 = 2 * (uint64_t)m0;
@@ -79,22 +79,22 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
     bool G, P;
     limbs_from_sums<kCarryLimbs>(T, prev_hi, v, gbits, G, P);
 
-    uint32_t* agg = args.scratch + 1;
+    uint32_t* agg = PP.scratch + 1;
     auto cin_fn = [&](bool Gb, bool Pb) -> bool {
         agg[bid] = (Gb ? 1u : 0u) | (Pb ? 2u : 0u);
         return false;
     };
     const bool cin = block_carry(G, P, sh, cin_fn);
-    limbs_finish<kCarryLimbs>(m0, args.lout, v, gbits, cin, args.out);
+    limbs_finish<kCarryLimbs>(m0, PP.lout, v, gbits, cin, PP.out);
 
     // ---- phase 2: the last block resolves the carries between blocks
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&args.scratch[0], 1u) == (uint32_t)args.nblk - 1 ? 1u : 0u;
+    if (threadIdx.x == 0) s_last = atomicAdd(&PP.scratch[0], 1u) == (uint32_t)PP.nblk - 1 ? 1u : 0u;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    const int nblk = args.nblk;
+    const int nblk = PP.nblk;
     const int per = (nblk + blockDim.x - 1) / blockDim.x;  // aggregates per thread
     const int b0 = threadIdx.x * per;
     // this thread's run of blocks as one carry element
@@ -110,10 +110,10 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
         const uint32_t a = __ldcg(&agg[b]);
         if (c) {
             // the carry enters block b: +1 ripples through its all-ones limbs
-            const uint64_t lim_end = min((uint64_t)(b + 1) * kBlockLimbs, args.lout);
+            const uint64_t lim_end = min((uint64_t)(b + 1) * kBlockLimbs, PP.lout);
             for (uint64_t m = (uint64_t)b * kBlockLimbs; m < lim_end; ++m) {
-                const uint64_t x = __ldcg(&args.out[m]) + 1;
-                args.out[m] = x;
+                const uint64_t x = __ldcg(&PP.out[m]) + 1;
+                PP.out[m] = x;
                 if (x != 0) break;
             }
         }

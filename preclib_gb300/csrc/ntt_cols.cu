@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
-    select_product(args, batch);
+    const ProdPtrs P = select_product(args, batch);
     const int prime = blockIdx.y >> 1, operand = blockIdx.y & 1;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.tf[prime];
@@ -29,36 +29,23 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
 
     // the carry kernel's look-back words start at zero
     if (blockIdx.y == 0) {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= args.nblk; i += gridDim.x * blockDim.x)
-            args.scratch[i] = 0;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= P.nblk; i += gridDim.x * blockDim.x)
+            P.scratch[i] = 0;
     }
 
-    const uint32_t* __restrict__ dig = reinterpret_cast<const uint32_t*>(operand ? args.b : args.a);
-    const uint64_t nd = 2 * (operand ? args.lb : args.la);
-    {   // top pass straight from the limbs
-        using G = Geom<M, 0>;
-        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
-            const int col = w & (C - 1);
-            const uint32_t u = w / C;
-            const uint32_t base = G::base(u);
-            uint32_t x[1][G::R];
-#pragma unroll
-            for (int q = 0; q < G::R; ++q) {
-                const uint64_t d = (uint64_t)(base + ((uint32_t)q << G::LO)) * N2 + c0 + col;
-                x[0][q] = d < nd ? Ar<SET>::digit(__ldg(&dig[d]), pc) : 0u;
-            }
-            regs_pass<SET, M, 0, false, 1>(x, u, tw, pc);
-            uint32_t* s = sm + G::pbase(u) * C + col;
-#pragma unroll
-            for (int q = 0; q < G::R; ++q) s[q * G::QS * C] = x[0][q];
-        }
-        __syncthreads();
-    }
+    const uint32_t* __restrict__ dig = reinterpret_cast<const uint32_t*>(operand ? P.b : P.a);
+    const uint64_t nd = 2 * (operand ? P.lb : P.la);
+    // the column tile of raw digits, staged by 16-byte asynchronous copies
+    // (digits past the operand read as zero), then the top pass reduces them
+    stage_cols<M, C>(sm, dig, N2, c0, nd);
+    __syncthreads();
+    col_pass<SET, M, 0, false, C, true>(sm, tw, pc);
+    __syncthreads();
     col_passes<SET, M, 1, NP - 2, false, C>(sm, tw, pc);
     {   // bottom pass (bits 0..4) with the four-step twiddle, straight to HBM
         using G = Geom<M, NP - 1>;
         static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
-        uint32_t* __restrict__ dst = args.work + ((uint64_t)blockIdx.y << args.k);
+        uint32_t* __restrict__ dst = P.work + ((uint64_t)blockIdx.y << args.k);
         for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
             const int col = w & (C - 1);
             const uint32_t u = w / C;
@@ -89,29 +76,17 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
-    select_product(args, batch);
+    const ProdPtrs P = select_product(args, batch);
     const int prime = blockIdx.y;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.ti[prime];
     const uint32_t N2 = 1u << args.k2;
     const uint32_t c0 = blockIdx.x * C;
-    uint32_t* __restrict__ wk = args.work + ((uint64_t)(prime * 2) << args.k);
-    {   // bottom DIT pass (bits 0..4 of the slot) straight from HBM
-        using G = Geom<M, NP - 1>;
-        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
-            const int col = w & (C - 1);
-            const uint32_t u = w / C;
-            uint32_t x[1][32];
-#pragma unroll
-            for (int q = 0; q < 32; ++q) x[0][q] = wk[(uint64_t)(32 * u + q) * N2 + c0 + col];
-            regs_pass<SET, M, NP - 1, true, 1>(x, u, tw, pc);
-            uint32_t* s = sm + (33 * u) * C + col;
-#pragma unroll
-            for (int q = 0; q < 32; ++q) s[q * C] = x[0][q];
-        }
-        __syncthreads();
-    }
-    col_passes<SET, M, NP - 2, 1, true, C>(sm, tw, pc);
+    uint32_t* __restrict__ wk = P.work + ((uint64_t)(prime * 2) << args.k);
+    // the column tile, staged by 16-byte asynchronous copies
+    stage_cols<M, C>(sm, wk, N2, c0, ~0ull);
+    __syncthreads();
+    col_passes<SET, M, NP - 1, 1, true, C>(sm, tw, pc);
     {   // top DIT pass: natural row order i1, straight to HBM
         using G = Geom<M, 0>;
         for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {

@@ -179,9 +179,51 @@ __device__ __forceinline__ void row_pass(uint32_t* sm, int astride, int narr, co
     }
 }
 
+// 16-byte asynchronous copy global -> shared; bytes past src_bytes (0..16)
+// are zero-filled and not read
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+// 4-byte asynchronous copy (src_bytes 0 or 4; 0 zero-fills without reading)
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Stages rows [0, 2^M) x columns [c0, c0+C) of a row-major u32 matrix with
+// row length `ld` into the column layout (element i of column c at
+// P(i)*C + c); `valid` = number of meaningful elements of the matrix
+// (row-major index), the rest read as zero.  16-byte copies when the
+// matrix starts on a 16-byte boundary (ld and c0 are multiples of 4), else
+// 4-byte copies: operand limb arrays are only guaranteed 8-byte aligned.
+template <int M, int C>
+__device__ __forceinline__ void stage_cols(uint32_t* sm, const uint32_t* __restrict__ g, uint64_t ld, uint64_t c0,
+                                           uint64_t valid) {
+    constexpr int Q = C / 4;
+    if (((uintptr_t)g & 15) == 0) {
+        for (int w = threadIdx.x; w < (Q << M); w += blockDim.x) {
+            const int r = w / Q, h = w % Q;
+            const uint64_t idx = (uint64_t)r * ld + c0 + 4 * h;
+            const int bytes = idx >= valid ? 0 : (valid - idx >= 4 ? 16 : (int)(valid - idx) * 4);
+            cp_async16(sm + padded(r) * C + 4 * h, bytes ? g + idx : g, bytes);
+        }
+    } else {
+        for (int w = threadIdx.x; w < (C << M); w += blockDim.x) {
+            const int r = w / C, col = w % C;
+            const uint64_t idx = (uint64_t)r * ld + c0 + col;
+            const bool in = idx < valid;
+            cp_async4(sm + padded(r) * C + col, in ? g + idx : g, in ? 4 : 0);
+        }
+    }
+    cp_async_wait_all();
+}
+
 // Column layout: C interleaved columns, element i of column c at
 // P(i)*C + c; lanes cover C adjacent columns (twiddle loads broadcast).
-template <int SET, int M, int T, bool DIT, int C>
+// DIGIT: the values are raw 32-bit digits, reduced on load.
+template <int SET, int M, int T, bool DIT, int C, bool DIGIT = false>
 __device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
     using G = Geom<M, T>;
     const int total = C << G::LGI;
@@ -191,7 +233,7 @@ __device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__
         uint32_t* s = sm + G::pbase(u) * C + col;
         uint32_t x[1][G::R];
 #pragma unroll
-        for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS * C];
+        for (int q = 0; q < G::R; ++q) x[0][q] = DIGIT ? Ar<SET>::digit(s[q * G::QS * C], c) : s[q * G::QS * C];
         regs_pass<SET, M, T, DIT, 1>(x, u, tw, c);
 #pragma unroll
         for (int q = 0; q < G::R; ++q) s[q * G::QS * C] = x[0][q];

@@ -60,20 +60,22 @@ struct ProdPtrs {
 
 #ifdef __CUDACC__
 // the product this CTA works on: the launch's own arguments, or entry
-// blockIdx.z of a batch's descriptor array
-__device__ __forceinline__ void select_product(ProdArgs& args, const ProdPtrs* __restrict__ batch) {
-    if (batch) {
-        const ProdPtrs& p = batch[blockIdx.z];
-        args.a = p.a;
-        args.b = p.b;
-        args.out = p.out;
-        args.work = p.work;
-        args.scratch = p.scratch;
-        args.la = p.la;
-        args.lb = p.lb;
-        args.lout = p.lout;
-        args.nblk = p.nblk;
-    }
+// blockIdx.z of a batch's descriptor array (a separate value, so the kernel
+// parameter block is never written and stays in the constant bank)
+__device__ __forceinline__ ProdPtrs select_product(const ProdArgs& args, const ProdPtrs* __restrict__ batch) {
+    if (batch) return batch[blockIdx.z];
+    ProdPtrs p;
+    p.a = args.a;
+    p.b = args.b;
+    p.out = args.out;
+    p.work = args.work;
+    p.scratch = args.scratch;
+    p.la = args.la;
+    p.lb = args.lb;
+    p.lout = args.lout;
+    p.nblk = args.nblk;
+    p.pad = 0;
+    return p;
 }
 #endif
 

@@ -17,13 +17,13 @@ __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, con
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "row transforms have at least two passes");
     constexpr int AS = astride_for(M);
-    select_product(args, batch);
+    const ProdPtrs P = select_product(args, batch);
     const int prime = blockIdx.y;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ twf = args.f.tf[prime];
     const uint2* __restrict__ twi = args.f.ti[prime];
     const int rows = args.rows;
-    uint32_t* __restrict__ A = args.work + ((uint64_t)(prime * 2) << args.k);
+    uint32_t* __restrict__ A = P.work + ((uint64_t)(prime * 2) << args.k);
     const uint32_t* __restrict__ B = A + (1ull << args.k);
     const uint32_t row0 = blockIdx.x * rows;
 

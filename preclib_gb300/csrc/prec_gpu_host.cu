@@ -428,10 +428,12 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     Plan pl;
     if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl))) return r;
     if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
-    if ((r = ensure_io(c, 2 * lout))) return r;
+    // operands and result each start on a 256-byte boundary (32 limbs)
+    const size_t la_pad = (la + 31) & ~(size_t)31, lb_pad = (lb + 31) & ~(size_t)31;
+    if ((r = ensure_io(c, la_pad + lb_pad + lout))) return r;
     uint64_t* d_a = c.io;
-    uint64_t* d_b = c.io + la;
-    uint64_t* d_out = c.io + lout;
+    uint64_t* d_b = c.io + la_pad;
+    uint64_t* d_out = c.io + la_pad + lb_pad;
     cudaStream_t st = c.stream;
     CK(cudaStreamWaitEvent(st, c.last_done, 0));
     CK(cudaMemcpyAsync(d_a, a, la * sizeof(uint64_t), cudaMemcpyHostToDevice, st));

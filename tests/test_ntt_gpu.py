@@ -141,6 +141,24 @@ def test_device_api_matches_host_api(gpu):
         assert np.array_equal(got, O.mul_ntt(a, b))
 
 
+def test_device_api_odd_limb_offsets(gpu):
+    """Operands that start 8 bytes past a 16-byte boundary (any limb offset
+    of a device array is a valid operand)."""
+    torch = pytest.importorskip("torch")
+    for (an, bn) in ((40000, 30001), (2049, 2039), (300, 7)):
+        a = O.splitmix64(an + 5, an)
+        b = O.splitmix64(bn + 6, bn)
+        buf = torch.empty(an + bn + 3, dtype=torch.int64, device="cuda")
+        buf[1:1 + an] = torch.from_numpy(a.view(np.int64)).cuda()
+        buf[2 + an:2 + an + bn] = torch.from_numpy(b.view(np.int64)).cuda()
+        to = torch.empty(an + bn + 1, dtype=torch.int64, device="cuda")
+        pa, pb, po = buf.data_ptr() + 8, buf.data_ptr() + 8 * (2 + an), to.data_ptr() + 8
+        gpu.mul_device(pa, an, pb, bn, po)
+        gpu.stream_check()
+        got = to[1:].cpu().numpy().view(np.uint64)
+        assert np.array_equal(got, O.mul_ntt(a, b)), (an, bn)
+
+
 def test_too_large_rejected(gpu):
     a = np.ones(1, np.uint64)
     with pytest.raises(gpu.PrecGpuError) as e:

@@ -87,10 +87,14 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
     const bool cin = block_carry(G, P, sh, cin_fn);
     limbs_finish<kCarryLimbs>(m0, PP.lout, v, gbits, cin, PP.out);
 
-    // ---- phase 2: the last block resolves the carries between blocks
-    __threadfence();
+    // ---- phase 2: the last block resolves the carries between blocks.
+    // The barrier orders every thread's limb and aggregate stores before
+    // thread 0's device-scope fence, which orders them before the counter.
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&PP.scratch[0], 1u) == (uint32_t)PP.nblk - 1 ? 1u : 0u;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&PP.scratch[0], 1u) == (uint32_t)PP.nblk - 1 ? 1u : 0u;
+    }
     __syncthreads();
     if (!s_last) return;
     __threadfence();

@@ -77,6 +77,14 @@ int prec_gpu_mul_ntt(const uint64_t *a, size_t an, const uint64_t *b, size_t bn,
  * that precn_sqr sends to mul_fft, src/mul_basic.cpp:203) run the NTT band. */
 int prec_gpu_mul_fft(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uint64_t *out);
 
+/* Square of a host limb vector, out[0 .. 2an) written (replaces precn_sqr,
+ * src/mul_basic.cpp:193-204, above its schoolbook base case).  The operand
+ * is copied to the device once and, on the NTT band's four-step path,
+ * transformed once per prime (a product transforms both operands).
+ * prec_gpu_mul, prec_gpu_mul_ntt and
+ * prec_gpu_mul_device take the same route when a == b and an == bn. */
+int prec_gpu_sqr(const uint64_t *a, size_t an, uint64_t *out);
+
 /* Digit width (bits) the FP64 band uses for an x bn limbs; 0 outside the band. */
 int prec_gpu_fft_digit_bits(size_t an, size_t bn);
 

@@ -146,6 +146,14 @@ def ref_mul_basic(a, b, variant=""):
     return _call(ref_lib(variant).ref_mul_basic, a, b)
 
 
+def ref_sqr(a, variant=""):
+    """The reference's precn_sqr (src/mul_basic.cpp:193-204)."""
+    a = _c(a)
+    out = np.zeros(max(2 * len(a), 1), dtype=np.uint64)
+    ref_lib(variant).ref_sqr(_ptr(a), len(a), _ptr(out))
+    return out[: 2 * len(a)]
+
+
 def ref_mul_fft(a, b, variant=""):
     a, b = _c(a), _c(b)
     out = np.zeros(max(len(a) + len(b), 1), dtype=np.uint64)

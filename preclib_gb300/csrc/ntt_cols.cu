@@ -21,7 +21,9 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
     const ProdPtrs P = select_product(args, batch);
-    const int prime = blockIdx.y >> 1, operand = blockIdx.y & 1;
+    // grid.y: prime*2 + operand, or just the prime for a square (one operand)
+    const int prime = args.square ? blockIdx.y : blockIdx.y >> 1;
+    const int operand = args.square ? 0 : blockIdx.y & 1;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.tf[prime];
     const uint32_t N2 = 1u << args.k2;
@@ -45,7 +47,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     {   // bottom pass (bits 0..4) with the four-step twiddle, straight to HBM
         using G = Geom<M, NP - 1>;
         static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
-        uint32_t* __restrict__ dst = P.work + ((uint64_t)blockIdx.y << args.k);
+        uint32_t* __restrict__ dst = P.work + ((uint64_t)(prime * 2 + operand) << args.k);
         for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
             const int col = w & (C - 1);
             const uint32_t u = w / C;
@@ -117,7 +119,7 @@ static size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * siz
 
 void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
     const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, 2 * kPrimes, count);
+    const dim3 grid((1u << a.k2) / cg, (a.square ? 1 : 2) * kPrimes, count);
     const size_t smem = col_smem(m, cg);
 #define X(S, MM, CC) \
     if (set == S && m == MM) { k_fwd_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }

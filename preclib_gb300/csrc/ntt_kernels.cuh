@@ -39,7 +39,7 @@ struct ProdArgs {
     int k, k1, k2;      // log2 of N, of the column length N1, of the row length N2
     int nblk;           // blocks of the carry kernel
     int rows;           // rows per CTA of the row pass
-    int pad;
+    int square;         // a == b: one operand transform, pointwise square
     CrtConst crt;
     FieldArgs f;
 };
@@ -87,7 +87,7 @@ struct SmallDesc {
     uint64_t* out;
     uint64_t la, lb, lout;
     int k;
-    int pad;
+    int square;  // a == b: one operand transform, pointwise square
     CrtConst crt;
 };
 

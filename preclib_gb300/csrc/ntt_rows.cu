@@ -11,7 +11,7 @@
 
 namespace precgpu {
 
-template <int SET, int M>
+template <int SET, int M, bool SQ>
 __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M);
@@ -26,47 +26,49 @@ __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, con
     uint32_t* __restrict__ A = P.work + ((uint64_t)(prime * 2) << args.k);
     const uint32_t* __restrict__ B = A + (1ull << args.k);
     const uint32_t row0 = blockIdx.x * rows;
+    constexpr int NA = SQ ? 1 : 2;  // a square transforms its one operand only
 
-    {   // top DIF pass of A and B straight from HBM (shared twiddles)
+    {   // top DIF pass of A (and B) straight from HBM (shared twiddles)
         using G = Geom<M, 0>;
         for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
             const int r = w >> G::LGI;
             const uint32_t u = w & ((1u << G::LGI) - 1);
             const uint64_t roff = ((uint64_t)(row0 + r) << M) + G::base(u);
-            uint32_t x[2][G::R];
+            uint32_t x[NA][G::R];
 #pragma unroll
             for (int q = 0; q < G::R; ++q) {
                 x[0][q] = A[roff + ((uint32_t)q << G::LO)];
-                x[1][q] = B[roff + ((uint32_t)q << G::LO)];
+                if constexpr (!SQ) x[NA - 1][q] = B[roff + ((uint32_t)q << G::LO)];
             }
-            regs_pass<SET, M, 0, false, 2>(x, u, twf, pc);
+            regs_pass<SET, M, 0, false, NA>(x, u, twf, pc);
             uint32_t* s = sm + 2 * r * AS + G::pbase(u);
 #pragma unroll
             for (int q = 0; q < G::R; ++q) {
                 s[q * G::QS] = x[0][q];
-                s[AS + q * G::QS] = x[1][q];
+                if constexpr (!SQ) s[AS + q * G::QS] = x[NA - 1][q];
             }
         }
         __syncthreads();
     }
-    row_passes<SET, M, 1, NP - 2, false, 2>(sm, AS, 2 * rows, twf, pc);
-    {   // bottom: last DIF stages of A and B, product, first DIT stages
+    if constexpr (SQ) row_passes<SET, M, 1, NP - 2, false, 1>(sm, 2 * AS, rows, twf, pc);
+    else row_passes<SET, M, 1, NP - 2, false, 2>(sm, AS, 2 * rows, twf, pc);
+    {   // bottom: last DIF stages, product, first DIT stages
         using G = Geom<M, NP - 1>;
         static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
         for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
             const int r = w >> G::LGI;
             const uint32_t u = w & ((1u << G::LGI) - 1);
             uint32_t* s = sm + 2 * r * AS + 33 * u;
-            uint32_t x[2][32];
+            uint32_t x[NA][32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
                 x[0][q] = s[q];
-                x[1][q] = s[AS + q];
+                if constexpr (!SQ) x[NA - 1][q] = s[AS + q];
             }
-            regs_pass<SET, M, NP - 1, false, 2>(x, u, twf, pc);
+            regs_pass<SET, M, NP - 1, false, NA>(x, u, twf, pc);
             uint32_t y[1][32];
 #pragma unroll
-            for (int q = 0; q < 32; ++q) y[0][q] = Ar<SET>::mul(x[0][q], x[1][q], pc);
+            for (int q = 0; q < 32; ++q) y[0][q] = Ar<SET>::mul(x[0][q], x[NA - 1][q], pc);
             regs_pass<SET, M, NP - 1, true, 1>(y, u, twi, pc);
 #pragma unroll
             for (int q = 0; q < 32; ++q) s[q] = y[0][q];
@@ -118,23 +120,24 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
     return rows << (k2 - 5);
 }
 
-#define PREC_ROWS(X) X(0, 7) X(0, 8) X(0, 9) X(0, 10) X(0, 11) X(0, 12) X(1, 13)
+#define PREC_ROWS1(X, SQ) X(0, 7, SQ) X(0, 8, SQ) X(0, 9, SQ) X(0, 10, SQ) X(0, 11, SQ) X(0, 12, SQ) X(1, 13, SQ)
+#define PREC_ROWS(X) PREC_ROWS1(X, false) PREC_ROWS1(X, true)
 
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
     const int m = a.k2;
     const dim3 grid((1u << a.k1) / a.rows, kPrimes, count);
     const int threads = a.rows << (m - 5);
     const size_t smem = row_smem(m, a.rows);
-#define X(S, MM) \
-    if (set == S && m == MM) { k_rows<S, MM><<<grid, threads, smem, st>>>(a, batch); return; }
+#define X(S, MM, SQ) \
+    if (set == S && m == MM && (a.square != 0) == SQ) { k_rows<S, MM, SQ><<<grid, threads, smem, st>>>(a, batch); return; }
     PREC_ROWS(X)
 #undef X
 }
 
 int configure_rows() {
     cudaError_t e = cudaSuccess;
-#define X(S, MM)                                                                                   \
-    if (!e) e = cudaFuncSetAttribute(k_rows<S, MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+#define X(S, MM, SQ)                                                                                   \
+    if (!e) e = cudaFuncSetAttribute(k_rows<S, MM, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)row_smem(MM, 256 >> (MM - 5) > 0 ? 256 >> (MM - 5) : 1));
     PREC_ROWS(X)
 #undef X

@@ -37,6 +37,7 @@ struct Chunk {
 
 struct Cls {
     int k = 0;
+    int square = 0;               // every product of the class is a square
     Plan pl;                      // class-wide plan (k, set, k1, k2, rows, crt)
     std::vector<int> items;       // indices into the batch's products
     size_t ws_per = 0;            // workspace bytes per product (four-step)
@@ -116,6 +117,7 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
             args.k1 = c.pl.k1;
             args.k2 = c.pl.k2;
             args.rows = c.pl.rows;
+            args.square = c.square;
             args.crt = c.pl.crt;
             args.f = ctx_field(c.pl.set);
             for (const Chunk& ch : c.chunks)
@@ -139,7 +141,7 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
     prec_gpu_batch* b = new prec_gpu_batch();
     b->items.assign(items, items + count);
     b->err = ctx_device_err();
-    std::map<int, Cls> by_k;
+    std::map<int, Cls> by_k;  // key 2k + square
     for (size_t i = 0; i < count; ++i) {
         const prec_gpu_product_t& p = items[i];
         if ((p.an && !p.a) || (p.bn && !p.b) || (p.an + p.bn && !p.out)) {
@@ -155,9 +157,11 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
             batch_free(b);
             return r;
         }
-        Cls& c = by_k[pl.k];
+        const int sq = (p.a == p.b && p.an == p.bn && pl.path == 1) ? 1 : 0;
+        Cls& c = by_k[2 * pl.k + sq];
         if (c.items.empty()) {
             c.k = pl.k;
+            c.square = sq;
             c.pl = pl;
         }
         c.items.push_back((int)i);
@@ -200,7 +204,7 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
                 d.lb = p.bn;
                 d.lout = p.an + p.bn;
                 d.k = c.k;
-                d.pad = 0;
+                d.square = p.a == p.b && p.an == p.bn;
                 d.crt = c.pl.crt;
             }
             c.d_small = reinterpret_cast<SmallDesc*>(base + desc_off[ci]);

@@ -68,9 +68,9 @@ constexpr int kMaxStages = 8;
 static const char* const kStageNames[3][kMaxStages] = {
     {"k_small"},
     {"k_fwd_cols", "k_rows", "k_inv_cols", "k_crt_carry"},
-    {"k_fft"},
+    {"k_fft_fwd_cols", "k_fft_rows", "k_fft_inv_cols", "k_fft_carry"},
 };
-static const int kStageCount[3] = {1, 4, 1};
+static const int kStageCount[3] = {1, 4, 4};
 
 constexpr size_t kStatBytes = 16;       // device status block (error bits, FFT distance)
 constexpr size_t kFftBandMin = 192;     // src/mul_basic.cpp:4 (FFT above 192 limbs)
@@ -297,8 +297,11 @@ static int ensure_io(Ctx& c, size_t limbs) {
 }
 
 // Enqueues one NTT-band product on device pointers.
+// A square (d_a == d_b, la == lb) transforms its one operand only on the
+// four-step path; the single-CTA path reads the operand twice.
 static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
                        uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+    const int square = (d_a == d_b && la == lb) ? 1 : 0;
     const uint64_t lout = la + lb;
     if (pl.path == 0) {
         SmallDesc d;
@@ -309,7 +312,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         d.lb = lb;
         d.lout = lout;
         d.k = pl.k;
-        d.pad = 0;
+        d.square = square;
         d.crt = pl.crt;
         ntt_launch_small(nullptr, &d, 1, pl.k, c.field[0], st, ev);
     } else {
@@ -328,7 +331,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.k2 = pl.k2;
         args.nblk = pl.nblk;
         args.rows = pl.rows;
-        args.pad = 0;
+        args.square = square;
         args.crt = pl.crt;
         args.f = c.field[pl.set];
         ntt_launch_4step(pl.set, args, st, ev);
@@ -402,8 +405,11 @@ static bool fft_plan_for(uint64_t la, uint64_t lb, FftPlan& fp) {
 
 enum { kModeBands = 0, kModeNtt = 1, kModeFft = 2 };
 
+// A square (a == b, an == bn: the reference's &a == &b test,
+// src/mul_basic.cpp:244-246) copies its operand to the device once.
 static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out, int mode) {
     if ((!a && an) || (!b && bn) || (!out && an + bn)) return PREC_GPU_E_ARG;
+    const bool square = a == b && an == bn;
     Ctx& c = g_ctx;
     std::lock_guard<std::mutex> lk(c.mu);
     int r = init_locked(c, -1);
@@ -429,15 +435,15 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl))) return r;
     if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
     // operands and result each start on a 256-byte boundary (32 limbs)
-    const size_t la_pad = (la + 31) & ~(size_t)31, lb_pad = (lb + 31) & ~(size_t)31;
+    const size_t la_pad = (la + 31) & ~(size_t)31, lb_pad = square ? 0 : (lb + 31) & ~(size_t)31;
     if ((r = ensure_io(c, la_pad + lb_pad + lout))) return r;
     uint64_t* d_a = c.io;
-    uint64_t* d_b = c.io + la_pad;
+    uint64_t* d_b = square ? d_a : c.io + la_pad;
     uint64_t* d_out = c.io + la_pad + lb_pad;
     cudaStream_t st = c.stream;
     CK(cudaStreamWaitEvent(st, c.last_done, 0));
     CK(cudaMemcpyAsync(d_a, a, la * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    if (!square) CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(c.ev0, st));
     if (use_fft) {
         FftArgs f{};
@@ -531,6 +537,8 @@ int prec_gpu_mul_ntt(const uint64_t* a, size_t an, const uint64_t* b, size_t bn,
 int prec_gpu_mul_fft(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
     return host_mul(a, an, b, bn, out, kModeFft);
 }
+
+int prec_gpu_sqr(const uint64_t* a, size_t an, uint64_t* out) { return host_mul(a, an, a, an, out, kModeBands); }
 
 int prec_gpu_fft_digit_bits(size_t an, size_t bn) {
     FftPlan fp;

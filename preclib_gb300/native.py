@@ -26,6 +26,7 @@ EXPORTS = (
     "prec_gpu_fft_digit_bits", "prec_gpu_batch_create", "prec_gpu_batch_run", "prec_gpu_batch_info",
     "prec_gpu_batch_destroy", "prec_gpu_mul_batch", "prec_gpu_serve_create", "prec_gpu_serve_submit",
     "prec_gpu_serve_wait", "prec_gpu_serve_drain", "prec_gpu_serve_stats", "prec_gpu_serve_destroy",
+    "prec_gpu_sqr",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -74,6 +75,8 @@ def lib() -> ctypes.CDLL:
             f = getattr(L, name)
             f.argtypes = [_u64p, ctypes.c_size_t, _u64p, ctypes.c_size_t, _u64p]
             f.restype = ctypes.c_int
+        L.prec_gpu_sqr.argtypes = [_u64p, ctypes.c_size_t, _u64p]
+        L.prec_gpu_sqr.restype = ctypes.c_int
         L.prec_gpu_mul_device.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                           ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         L.prec_gpu_mul_device.restype = ctypes.c_int
@@ -159,6 +162,14 @@ def mul(a, b, ntt: bool = False, fft: bool = False) -> np.ndarray:
     f = lib().prec_gpu_mul_ntt if ntt else (lib().prec_gpu_mul_fft if fft else lib().prec_gpu_mul)
     check(f(_p(a), len(a), _p(b), len(b), _p(out)), "prec_gpu_mul")
     return out[: len(a) + len(b)]
+
+
+def sqr(a) -> np.ndarray:
+    """Square of a host limb vector (2*len(a) limbs), computed on the GPU."""
+    a = _arr(a)
+    out = np.empty(max(2 * len(a), 1), dtype=np.uint64)
+    check(lib().prec_gpu_sqr(_p(a), len(a), _p(out)), "prec_gpu_sqr")
+    return out[: 2 * len(a)]
 
 
 def mul_device(a_ptr: int, an: int, b_ptr: int, bn: int, out_ptr: int, stream: int = 0) -> None:

@@ -31,7 +31,9 @@ def digest(out: np.ndarray) -> str:
 
 def record(name, gen, fn):
     a, b = patterns.make(gen)
-    if fn == "fft":
+    if fn == "sqr":
+        out, err = O.ref_sqr(a), None
+    elif fn == "fft":
         out, err = O.ref_mul_fft(a, b)
     elif fn == "ntt":
         out, err = O.ref_mul_ntt(a, b), None
@@ -78,6 +80,13 @@ def main():
     for (an, bn, s) in ((6145, 6145, 40), (6145, 12290, 41), (12289, 7000, 42), (20000, 10001, 43),
                         (100000, 77777, 44), (262144, 262144, 45), (300000, 150001, 46)):
         recs.append(record("edge_%dx%d_ntt" % (an, bn), dict(kind="splitmix64", seed_a=s, seed_b=s + 100, an=an, bn=bn), "ntt"))
+    # precn_sqr (src/mul_basic.cpp:193-204): mul_fft(a, a) above 192 limbs at
+    # every size, Karatsuba below; the operand is `a` of the generator
+    for (an, s) in ((100, 60), (193, 61), (3000, 62), (6144, 63), (6145, 64), (8192, 65), (20000, 66),
+                    (65536, 67), (1 << 18, 68)):
+        recs.append(record("sqr_%d" % an, dict(kind="splitmix64", seed_a=s, seed_b=s, an=an, bn=an), "sqr"))
+    for an in (6144, 20000):
+        recs.append(record("sqr_ones_%d" % an, dict(kind="torture", pattern="all-ones", an=an, bn=an), "sqr"))
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "products.json")
     with open(path, "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "reference": "preclib src/*.cpp (g++ -O3, COUNT_FFTS=1)",

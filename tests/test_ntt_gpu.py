@@ -20,6 +20,8 @@ def test_golden_vectors_ntt(gpu, golden):
     product is an exact integer) through the NTT band."""
     for rec in golden:
         a, b = patterns.make(rec["gen"])
+        if rec["ref_fn"] == "sqr":
+            b = a  # the same vector: the square route
         out = gpu.mul(a, b, ntt=True)
         assert _digest(out) == rec["sha256"], rec["name"]
 

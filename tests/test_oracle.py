@@ -19,7 +19,9 @@ def test_golden_vectors(golden):
     FFT restatement reproduces the reference's rounding distances."""
     for rec in golden:
         a, b = patterns.make(rec["gen"])
-        if rec["ref_fn"] == "ntt":
+        if rec["ref_fn"] == "sqr":
+            out = O.mul_ntt(a, a)  # an exact square, whichever band made it
+        elif rec["ref_fn"] == "ntt":
             out = O.mul_ntt(a, b)
         elif rec["ref_fn"] == "fft":
             out, err = O.mul_fft(a, b)

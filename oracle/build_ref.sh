@@ -5,6 +5,9 @@
 # nothing and exits 0 when it is absent.  Outputs go only to oracle/_ref/.
 #   libprecref.so       portable build (-O3, no SIMD flags), COUNT_FFTS on
 #   libprecref_avx2.so  x86-64 only: -mavx2 build, for the CPU-baseline table
+#   interposed/         (argument "interposed") preclib's fft_torture,
+#                       test_opt_smoke and pi_chudnovsky linked with the GPU
+#                       mul_ntt / mul_fft instead of src/mul_ntt.cpp, mul_fft.cpp
 set -euo pipefail
 REF=${PRECLIB_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -14,6 +17,13 @@ if [ ! -f "$REF/prec.hpp" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
+if [ "${1:-}" = "interposed" ]; then
+  # preclib's own programs with mul_ntt/mul_fft from the GPU library
+  # (needs preclib_gb300/lib/libprecgpu.so built first)
+  "$HERE/../preclib_gb300/precn/link_preclib.sh" "$REF" "$OUT/interposed" \
+    "$REF/test/fft_torture.cpp" "$REF/test/test_opt_smoke.cpp" "$REF/pi/pi_chudnovsky.cpp"
+  exit 0
+fi
 CXX=${CXX:-g++}
 SRCS=("$REF"/src/*.cpp)
 "$CXX" -O3 -std=c++17 -fPIC -shared -DCOUNT_FFTS=1 -I"$REF" \

@@ -21,15 +21,27 @@
 #ifndef PREC_COLS_MINB
 #define PREC_COLS_MINB 3
 #endif
+// unroll factor of the item loops of the shared-memory passes
+#ifndef PREC_PASS_UNROLL
+#define PREC_PASS_UNROLL 1
+#endif
 
 namespace precgpu {
 
 typedef unsigned __int128 u128;
 
+constexpr int kPassUnroll = PREC_PASS_UNROLL;
+
 // ---------------------------------------------------------------------------
 // compile-time pass schedule (t = 0 is the top pass, t = np-1 the bottom)
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int sch_np(int m) { return m <= 5 ? 1 : 1 + (m - 5 + 3) / 4; }
+#ifndef PREC_SCH_MAXRB
+#define PREC_SCH_MAXRB 4
+#endif
+// passes above the bottom one cover at most PREC_SCH_MAXRB bits each
+__host__ __device__ constexpr int sch_np(int m) {
+    return m <= 5 ? 1 : 1 + (m - 5 + PREC_SCH_MAXRB - 1) / PREC_SCH_MAXRB;
+}
 __host__ __device__ constexpr int sch_rb(int m, int t) {
     return m <= 5 ? m
                   : (t == sch_np(m) - 1 ? 5
@@ -162,6 +174,7 @@ __device__ __forceinline__ void row_pass(uint32_t* sm, int astride, int narr, co
                                          const PrimeC& c) {
     using G = Geom<M, T>;
     const int total = (narr / NA) << G::LGI;
+#pragma unroll kPassUnroll
     for (int w = threadIdx.x; w < total; w += blockDim.x) {
         const uint32_t u = w & ((1u << G::LGI) - 1);
         const int g = w >> G::LGI;
@@ -227,6 +240,7 @@ template <int SET, int M, int T, bool DIT, int C, bool DIGIT = false>
 __device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
     using G = Geom<M, T>;
     const int total = C << G::LGI;
+#pragma unroll kPassUnroll
     for (int w = threadIdx.x; w < total; w += blockDim.x) {
         const int col = w & (C - 1);
         const uint32_t u = w / C;

@@ -98,8 +98,15 @@ constexpr int kDevErrCarry = 2;
 constexpr int kSmallMaxLog2 = 12;
 constexpr int kSmallMinLog2 = 5;
 constexpr int kCarryThreads = 256;
-constexpr int kCarryLimbs = 4;  // limbs per thread in the carry kernel
-constexpr int kColGroup = 8;    // adjacent columns per column-pass CTA (4 when N1 = 2^13)
+// build-time tunables (defaults are the measured best on GB300)
+#ifndef PREC_CARRY_LIMBS
+#define PREC_CARRY_LIMBS 4
+#endif
+#ifndef PREC_COL_GROUP
+#define PREC_COL_GROUP 8
+#endif
+constexpr int kCarryLimbs = PREC_CARRY_LIMBS;  // limbs per thread in the carry kernel
+constexpr int kColGroup = PREC_COL_GROUP;      // adjacent columns per column-pass CTA (4 when N1 = 2^13)
 
 // host-side launchers; `ev` (optional) gets an event recorded before the
 // first kernel and after each kernel.

@@ -141,7 +141,24 @@ void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch
     launch_crt_carry(set, args, st, batch, count, max_nblk);
 }
 
-void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev) {
+void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev, const PrimeStreams* ps) {
+    if (ps && !ev) {
+        // one chain per prime; the CRT kernel joins them
+        cudaEventRecord(ps->fork, st);
+        for (int p = 0; p < kPrimes; ++p) {
+            cudaStream_t s = ps->s[p];
+            cudaStreamWaitEvent(s, ps->fork, 0);
+            ProdArgs a = args;
+            a.prime0 = p;
+            launch_fwd_cols(set, a, s, nullptr, 1, 1);
+            launch_rows(set, a, s, nullptr, 1, 1);
+            launch_inv_cols(set, a, s, nullptr, 1, 1);
+            cudaEventRecord(ps->join[p], s);
+            cudaStreamWaitEvent(st, ps->join[p], 0);
+        }
+        launch_crt_carry(set, args, st);
+        return;
+    }
     if (ev) cudaEventRecord(ev[0], st);
     launch_fwd_cols(set, args, st);
     if (ev) cudaEventRecord(ev[1], st);

@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     static_assert(NP >= 2, "column transforms have at least two passes");
     const ProdPtrs P = select_product(args, batch);
     // grid.y: prime*2 + operand, or just the prime for a square (one operand)
-    const int prime = args.square ? blockIdx.y : blockIdx.y >> 1;
+    const int prime = args.prime0 + (args.square ? blockIdx.y : blockIdx.y >> 1);
     const int operand = args.square ? 0 : blockIdx.y & 1;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.tf[prime];
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     const uint32_t c0 = blockIdx.x * C;
 
     // the carry kernel's look-back words start at zero
-    if (blockIdx.y == 0) {
+    if (blockIdx.y == 0 && args.prime0 == 0) {
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= P.nblk; i += gridDim.x * blockDim.x)
             P.scratch[i] = 0;
     }
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
     constexpr int NP = sch_np(M);
     static_assert(NP >= 2, "column transforms have at least two passes");
     const ProdPtrs P = select_product(args, batch);
-    const int prime = blockIdx.y;
+    const int prime = args.prime0 + blockIdx.y;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.ti[prime];
     const uint32_t N2 = 1u << args.k2;
@@ -128,9 +128,9 @@ static size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * siz
     X(0, 11, kColGroup)
 #define PREC_COLS_SET1(X) X(1, 11, kColGroup) X(1, 12, 4) X(1, 13, 4)
 
-void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
     const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, (a.square ? 1 : 2) * kPrimes, count);
+    const dim3 grid((1u << a.k2) / cg, (a.square ? 1 : 2) * nprimes, count);
     const size_t smem = col_smem(m, cg);
 #define X(S, MM, CC) \
     if (set == S && m == MM) { k_fwd_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }
@@ -138,9 +138,9 @@ void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
 #undef X
 }
 
-void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
+void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
     const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, kPrimes, count);
+    const dim3 grid((1u << a.k2) / cg, nprimes, count);
     const size_t smem = col_smem(m, cg);
 #define X(S, MM, CC) \
     if (set == S && m == MM) { k_inv_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }

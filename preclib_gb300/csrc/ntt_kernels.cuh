@@ -40,6 +40,8 @@ struct ProdArgs {
     int nblk;           // blocks of the carry kernel
     int rows;           // rows per CTA of the row pass
     int square;         // a == b: one operand transform, pointwise square
+    int prime0;         // first prime of this launch of the transform kernels (grid.y covers the rest)
+    int pad;
     CrtConst crt;
     FieldArgs f;
 };
@@ -114,7 +116,16 @@ size_t ntt_small_smem_bytes(int k);
 int ntt_small_threads(int k);
 void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k,
                       const FieldArgs& f, cudaStream_t st, cudaEvent_t* ev = nullptr);
-void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev = nullptr);
+// Side streams of a single product: the three primes' transform kernels
+// run as independent chains (fork from and join to the caller's stream), so
+// one prime's tail wave overlaps another prime's work.
+struct PrimeStreams {
+    cudaStream_t s[kPrimes];
+    cudaEvent_t fork;
+    cudaEvent_t join[kPrimes];
+};
+void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                      const PrimeStreams* ps = nullptr);
 // the batch form: `count` products of one length class (class-wide fields
 // from `args`, per-product fields from the device array `batch`);
 // max_nblk = the largest carry grid of the class
@@ -124,9 +135,13 @@ int ntt_row_threads(int k2, int n1, int* rows);
 int ntt_configure_kernels();  // opt-in shared-memory sizes; returns a cudaError_t
 
 // launchers of each translation unit (ntt_cols.cu, ntt_rows.cu, ntt_carry.cu, ntt_small.cu)
-void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1);
-void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1);
-void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1);
+// (primes a.prime0 .. a.prime0 + nprimes - 1)
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
+                     int nprimes = kPrimes);
+void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
+                 int nprimes = kPrimes);
+void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
+                     int nprimes = kPrimes);
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
                       int max_nblk = 0);
 int configure_cols();

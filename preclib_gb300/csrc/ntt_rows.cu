@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, con
     static_assert(NP >= 2, "row transforms have at least two passes");
     constexpr int AS = astride_for(M);
     const ProdPtrs P = select_product(args, batch);
-    const int prime = blockIdx.y;
+    const int prime = args.prime0 + blockIdx.y;
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ twf = args.f.tf[prime];
     const uint2* __restrict__ twi = args.f.ti[prime];
@@ -144,9 +144,9 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
 #define PREC_ROWS1(X, SQ) X(0, 7, SQ) X(0, 8, SQ) X(0, 9, SQ) X(0, 10, SQ) X(0, 11, SQ) X(0, 12, SQ) X(1, 13, SQ)
 #define PREC_ROWS(X) PREC_ROWS1(X, false) PREC_ROWS1(X, true)
 
-void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count) {
+void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
     const int m = a.k2;
-    const dim3 grid((1u << a.k1) / a.rows, kPrimes, count);
+    const dim3 grid((1u << a.k1) / a.rows, nprimes, count);
     const int threads = a.rows << (m - 5);
     const size_t smem = row_smem(m, a.rows);
 #define X(S, MM, SQ) \

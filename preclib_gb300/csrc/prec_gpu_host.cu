@@ -141,9 +141,12 @@ struct Ctx {
     cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t stage_ev[kMaxStages + 1] = {};
     FieldArgs field[kSets] = {};
+    PrimeStreams prime_streams = {};
+    bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
 };
 
 static Ctx g_ctx;
+constexpr int kSplitMinLog2 = 19;  // smallest transform run as per-prime stream chains
 static thread_local prec_gpu_stats_t t_stats;
 
 int cuda_code(cudaError_t e) {
@@ -237,6 +240,15 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
     for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&c.stage_ev[i]));
+    for (int p = 0; p < kPrimes; ++p) {
+        CK(cudaStreamCreateWithFlags(&c.prime_streams.s[p], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c.prime_streams.join[p], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&c.prime_streams.fork, cudaEventDisableTiming));
+    {
+        const char* env = std::getenv("PREC_GPU_PRIME_STREAMS");
+        c.split_primes = !(env && env[0] == '0');
+    }
     CK(cudaMalloc(&c.d_err, kStatBytes));
     CK(cudaMemset(c.d_err, 0, kStatBytes));
     CK(cudaMallocHost(&c.h_err, kStatBytes));
@@ -316,7 +328,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         d.crt = pl.crt;
         ntt_launch_small(nullptr, &d, 1, pl.k, c.field[0], st, ev);
     } else {
-        ProdArgs args;
+        ProdArgs args{};
         args.a = d_a;
         args.b = d_b;
         args.out = d_out;
@@ -334,7 +346,10 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.square = square;
         args.crt = pl.crt;
         args.f = c.field[pl.set];
-        ntt_launch_4step(pl.set, args, st, ev);
+        // per-prime chains from 2^19 points up (below, the extra launches cost
+        // more than the overlapped tail waves save)
+        const bool split = c.split_primes && pl.k >= kSplitMinLog2;
+        ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr);
     }
     CK(cudaGetLastError());
     return 0;
@@ -518,6 +533,12 @@ void prec_gpu_shutdown(void) {
     cudaEventDestroy(c.ev0);
     cudaEventDestroy(c.ev1);
     for (int i = 0; i <= kMaxStages; ++i) cudaEventDestroy(c.stage_ev[i]);
+    for (int p = 0; p < kPrimes; ++p) {
+        cudaStreamDestroy(c.prime_streams.s[p]);
+        cudaEventDestroy(c.prime_streams.join[p]);
+    }
+    cudaEventDestroy(c.prime_streams.fork);
+    c.prime_streams = PrimeStreams{};
     cudaStreamDestroy(c.stream);
     c.ws = nullptr;
     c.io = nullptr;

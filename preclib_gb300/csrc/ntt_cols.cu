@@ -24,6 +24,34 @@
 
 namespace precgpu {
 
+// Top DIF pass of a digit tile whose upper half (rows 2^(M-1) and up) is
+// zero -- every operand of at most N/2 digits, i.e. both operands of a
+// balanced product: only the lower half is staged and reduced, and the
+// first stage (x, 0) -> (x, x*w) needs one twiddle product per pair.
+template <int SET, int M, int C>
+__device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
+    using G = Geom<M, 0>;
+    static_assert(G::LO >= 5, "the top pass of a multi-pass transform");
+    constexpr int H = G::R / 2;
+    for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+        const int col = w & (C - 1);
+        const uint32_t u = w / C;
+        const uint32_t ulo = u & G::LOMASK;
+        uint32_t* s = sm + G::pbase(u) * C + col;
+        uint32_t x[1][G::R];
+#pragma unroll
+        for (int q = 0; q < H; ++q) {
+            const uint32_t d = Ar<SET>::digit(s[q * G::QS * C], c);
+            const uint2 wq = __ldg(&tw[(1u << (G::LO + G::RB - 1)) + (ulo | ((uint32_t)q << G::LO))]);
+            x[0][q] = d;
+            x[0][q + H] = Ar<SET>::twiddle(d, wq, c);
+        }
+        dif_regs<SET, G::LO, G::RB, 1, G::RB - 2>(x, ulo, tw, c);
+#pragma unroll
+        for (int q = 0; q < G::R; ++q) s[q * G::QS * C] = x[0][q];
+    }
+}
+
 template <int SET, int M, int C>
 __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
@@ -48,9 +76,16 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     const uint64_t nd = 2 * (operand ? P.lb : P.la);
     // the column tile of raw digits, staged by 16-byte asynchronous copies
     // (digits past the operand read as zero), then the top pass reduces them
-    stage_cols<M, C>(sm, dig, N2, c0, nd);
-    __syncthreads();
-    col_pass<SET, M, 0, false, C, true>(sm, tw, pc);
+    if (nd <= (1ull << (args.k - 1))) {
+        stage_rows<M, C>(sm, dig, N2, c0, nd, 0, 1 << (M - 1));
+        cp_async_wait<0>();
+        __syncthreads();
+        col_top_upper_zero<SET, M, C>(sm, tw, pc);
+    } else {
+        stage_cols<M, C>(sm, dig, N2, c0, nd);
+        __syncthreads();
+        col_pass<SET, M, 0, false, C, true>(sm, tw, pc);
+    }
     __syncthreads();
     col_passes<SET, M, 1, NP - 2, false, C>(sm, tw, pc);
     {   // bottom pass (bits 0..4) with the four-step twiddle, straight to HBM

@@ -76,13 +76,14 @@ struct Geom {
 // register passes
 // ---------------------------------------------------------------------------
 
-// DIF stages over bits LO+RB-1 .. LO of NA arrays held in registers;
-// element q of an item sits at index base + (q << LO); ulo = base & LOMASK.
-template <int SET, int LO, int RB, int NA>
+// DIF stages over bits BTOP+LO .. LO of NA arrays held in registers
+// (BTOP = RB-1: all RB stages); element q of an item sits at index
+// base + (q << LO); ulo = base & LOMASK.
+template <int SET, int LO, int RB, int NA, int BTOP = RB - 1>
 __device__ __forceinline__ void dif_regs(uint32_t (&x)[NA][1 << RB], uint32_t ulo, const uint2* __restrict__ tw,
                                          const PrimeC& c) {
 #pragma unroll
-    for (int bb = RB - 1; bb >= 0; --bb) {
+    for (int bb = BTOP; bb >= 0; --bb) {
         const int h = 1 << bb;
         if constexpr (LO == 0) {
 #pragma unroll
@@ -204,6 +205,10 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// waits until at most N of this thread's committed groups are pending
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // Stages rows [0, 2^M) x columns [c0, c0+C) of a row-major u32 matrix with
 // row length `ld` into the column layout (element i of column c at
@@ -211,37 +216,48 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // (row-major index), the rest read as zero.  16-byte copies when the
 // matrix starts on a 16-byte boundary (ld and c0 are multiples of 4), else
 // 4-byte copies: operand limb arrays are only guaranteed 8-byte aligned.
+// stage_rows issues the copies of rows [r0, r1) only and commits them as
+// one group (cp_async_wait<n> then waits for all but the last n groups).
 template <int M, int C>
-__device__ __forceinline__ void stage_cols(uint32_t* sm, const uint32_t* __restrict__ g, uint64_t ld, uint64_t c0,
-                                           uint64_t valid) {
+__device__ __forceinline__ void stage_rows(uint32_t* sm, const uint32_t* __restrict__ g, uint64_t ld, uint64_t c0,
+                                           uint64_t valid, int r0, int r1) {
     constexpr int Q = C / 4;
     if (((uintptr_t)g & 15) == 0) {
-        for (int w = threadIdx.x; w < (Q << M); w += blockDim.x) {
+        for (int w = r0 * Q + threadIdx.x; w < r1 * Q; w += blockDim.x) {
             const int r = w / Q, h = w % Q;
             const uint64_t idx = (uint64_t)r * ld + c0 + 4 * h;
             const int bytes = idx >= valid ? 0 : (valid - idx >= 4 ? 16 : (int)(valid - idx) * 4);
             cp_async16(sm + padded(r) * C + 4 * h, bytes ? g + idx : g, bytes);
         }
     } else {
-        for (int w = threadIdx.x; w < (C << M); w += blockDim.x) {
+        for (int w = r0 * C + threadIdx.x; w < r1 * C; w += blockDim.x) {
             const int r = w / C, col = w % C;
             const uint64_t idx = (uint64_t)r * ld + c0 + col;
             const bool in = idx < valid;
             cp_async4(sm + padded(r) * C + col, in ? g + idx : g, in ? 4 : 0);
         }
     }
-    cp_async_wait_all();
+    cp_async_commit();
+}
+
+template <int M, int C>
+__device__ __forceinline__ void stage_cols(uint32_t* sm, const uint32_t* __restrict__ g, uint64_t ld, uint64_t c0,
+                                           uint64_t valid) {
+    stage_rows<M, C>(sm, g, ld, c0, valid, 0, 1 << M);
+    cp_async_wait<0>();
 }
 
 // Column layout: C interleaved columns, element i of column c at
 // P(i)*C + c; lanes cover C adjacent columns (twiddle loads broadcast).
-// DIGIT: the values are raw 32-bit digits, reduced on load.
+// DIGIT: the values are raw 32-bit digits, reduced on load.  Items
+// [w0, w1) of the pass (w1 < 0: all C << LGI items).
 template <int SET, int M, int T, bool DIT, int C, bool DIGIT = false>
-__device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
+__device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c, int w0 = 0,
+                                         int w1 = -1) {
     using G = Geom<M, T>;
-    const int total = C << G::LGI;
+    const int total = w1 < 0 ? (C << G::LGI) : w1;
 #pragma unroll kPassUnroll
-    for (int w = threadIdx.x; w < total; w += blockDim.x) {
+    for (int w = w0 + threadIdx.x; w < total; w += blockDim.x) {
         const int col = w & (C - 1);
         const uint32_t u = w / C;
         uint32_t* s = sm + G::pbase(u) * C + col;

@@ -116,6 +116,10 @@ struct Ar<0> {
     static __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b, const PrimeC& c) {
         return mont_lazy(a, b, c);
     }
+    // x * w for a table twiddle, any 32-bit x -> [0, 2p)
+    static __device__ __forceinline__ uint32_t twiddle(uint32_t x, uint2 w, const PrimeC& c) {
+        return shoup_lazy(x, w.x, w.y, c.p);
+    }
     // inverse-range value [0, 4p) -> forward range [0, 2p)
     static __device__ __forceinline__ uint32_t half(uint32_t x, const PrimeC& c) {
         return min(x, x - c.p2);
@@ -155,6 +159,9 @@ struct Ar<1> {
     }
     static __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b, const PrimeC& c) {
         return red1(mont_lazy(a, b, c), c.p);
+    }
+    static __device__ __forceinline__ uint32_t twiddle(uint32_t x, uint2 w, const PrimeC& c) {
+        return red1(shoup_lazy(x, w.x, w.y, c.p), c.p);
     }
     static __device__ __forceinline__ uint32_t half(uint32_t x, const PrimeC&) { return x; }
 };

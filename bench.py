@@ -377,6 +377,12 @@ def run_batch(args):
     d_out = torch.empty(o, dtype=torch.int64, device=dev)
     bi, bo = d_in.data_ptr(), d_out.data_ptr()
     items = [(bi + 8 * off, a, bi + 8 * (off + a), b, bo + 8 * off) for off, (a, b) in zip(offs, sizes)]
+    # kernel configuration of every four-step length class of the batch
+    # picked by the autotuner before the batch is planned (untimed)
+    kmax = max(native.ntt_log2(a, b) for a, b in sizes)
+    t_tune = time.perf_counter()
+    tuned = native.autotune(13, kmax)
+    tune_s = time.perf_counter() - t_tune
     batch = native.Batch(items)
     ncls, nbytes = batch.info()
 
@@ -445,6 +451,10 @@ def run_batch(args):
                    "plain_products_per_s": round(n / plain_dev_s, 1),
                    "batched_vs_plain": round(plain_dev_s / batched_dev_s, 2)},
         "mismatches_vs_plain": int(mismatches),
+        "autotune": {"seconds": round(tune_s, 3),
+                     "classes": {str(t["log2_n"]): [t["log2_cols"], t["col_group"], t["col_radix_cap"],
+                                                    t["rows_per_cta"], t["split_primes"]] for t in tuned},
+                     "fields": "log2_cols, col_group, col_radix_cap, rows_per_cta, split_primes"},
         "e2e": {"value": round(n / batched_s, 1), "unit": "products/s", "h2d_bytes_per_step": 8 * o,
                 "d2h_bytes_per_step": 8 * o},
         "gpu_launches": None,

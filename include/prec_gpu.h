@@ -85,6 +85,48 @@ int prec_gpu_mul_fft(const uint64_t *a, size_t an, const uint64_t *b, size_t bn,
  * prec_gpu_mul_device take the same route when a == b and an == bn. */
 int prec_gpu_sqr(const uint64_t *a, size_t an, uint64_t *out);
 
+/* ---- Autotuner ------------------------------------------------------------
+ * Kernel configuration of one four-step NTT length 2^log2_n (13 .. 26):
+ * the column/row split, columns per column-pass CTA, the column pass radix
+ * cap, rows per row-pass CTA, and whether a single product runs each
+ * prime's kernels on its own stream.  Every product (single, batch,
+ * serving loop) uses the configuration of its length.  Defaults apply until
+ * a length is tuned, set or loaded; PREC_GPU_TUNE_FILE names a table that
+ * prec_gpu_init loads. */
+typedef struct {
+    int log2_n;
+    int log2_cols;      /* column length 2^log2_cols, row length 2^(log2_n - log2_cols) */
+    int col_group;      /* columns per column-pass CTA: 4 or 8 */
+    int col_radix_cap;  /* largest radix 2^cap of a column pass: 4 or 6 */
+    int rows_per_cta;   /* rows per row-pass CTA */
+    int split_primes;   /* 1: per-prime stream chains for a single product */
+    float ms;           /* measured product time (0: not measured) */
+    float default_ms;   /* the default configuration's time (0: not measured) */
+} prec_gpu_tune_entry_t;
+
+/* Times the configurations of every length 2^kmin .. 2^kmax (clamped to
+ * 13 .. 26) on the current device with balanced random operands of
+ * 2^(k-2) limbs each, by coordinate descent from the default (per-prime
+ * streams, rows per CTA, columns per CTA, radix cap, then the column/row
+ * split).  A candidate counts only if its product equals the default
+ * configuration's bit for bit; the fastest is installed.  Writes up to
+ * `cap` entries to `out` (may be NULL) and the number of lengths to *count. */
+int prec_gpu_autotune(int kmin, int kmax, prec_gpu_tune_entry_t *out, size_t cap, size_t *count);
+
+/* The configuration length 2^log2_n uses now (tuned, set, loaded or default). */
+int prec_gpu_tune_get(int log2_n, prec_gpu_tune_entry_t *entry);
+
+/* Installs a configuration; PREC_GPU_E_ARG if no kernel exists for it. */
+int prec_gpu_tune_set(const prec_gpu_tune_entry_t *entry);
+
+/* Every length back to its default configuration. */
+int prec_gpu_tune_reset(void);
+
+/* The table as text, one line per tuned length.  Loading validates every
+ * line and installs nothing if one is invalid (PREC_GPU_E_ARG). */
+int prec_gpu_tune_save(const char *path);
+int prec_gpu_tune_load(const char *path);
+
 /* Digit width (bits) the FP64 band uses for an x bn limbs; 0 outside the band. */
 int prec_gpu_fft_digit_bits(size_t an, size_t bn);
 

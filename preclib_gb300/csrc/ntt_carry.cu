@@ -171,7 +171,8 @@ void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_
 }
 
 int ntt_configure_kernels() {
-    int e = configure_cols();
+    int e = configure_fwd_cols();
+    if (!e) e = configure_inv_cols();
     if (!e) e = configure_rows();
     if (!e) e = configure_small();
     return e;

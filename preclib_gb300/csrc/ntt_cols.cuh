@@ -1,4 +1,4 @@
-// ntt_cols.cu -- column passes of the four-step NTT (index i = i1*N2 + i2).
+// ntt_cols.cuh -- column passes of the four-step NTT (index i = i1*N2 + i2).
 //
 // k_fwd_cols: for C adjacent columns i2 of one operand and one prime, the
 //   limbs are read as 32-bit digits (the reference's ntt_digits and mont_in,
@@ -11,26 +11,24 @@
 // Columns are interleaved in shared memory (element i of column c at
 // P(i)*C + c); a warp covers C columns x 32/C items, so every global access
 // moves whole 32-byte sectors.
-// pass radix cap of the column transforms: a 2^11-point column runs as a
-// radix-64 and a radix-32 pass (one shared-memory round trip fewer than
-// with radix-8 passes; 11% faster forward columns on GB300)
-#ifndef PREC_COLS_MAXRB
-#define PREC_COLS_MAXRB 6
-#endif
-#ifndef PREC_SCH_MAXRB
-#define PREC_SCH_MAXRB PREC_COLS_MAXRB
-#endif
+// Template parameters: SET prime set, M = log2 N1 (column length), C
+// columns per CTA, MR the pass radix cap (MR = 6: a 2^11-point column runs
+// as a radix-64 and a radix-32 pass; MR = 4: radix-8, -8, -32).  The
+// instantiated (SET, M, C, MR) configurations are PREC_COLS_CONFIGS; the
+// autotuner picks C and MR per transform length.
+#pragma once
 #include "ntt_engine.cuh"
 
 namespace precgpu {
+
 
 // Top DIF pass of a digit tile whose upper half (rows 2^(M-1) and up) is
 // zero -- every operand of at most N/2 digits, i.e. both operands of a
 // balanced product: only the lower half is staged and reduced, and the
 // first stage (x, 0) -> (x, x*w) needs one twiddle product per pair.
-template <int SET, int M, int C>
+template <int SET, int M, int C, int MR>
 __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
-    using G = Geom<M, 0>;
+    using G = Geom<M, 0, MR>;
     static_assert(G::LO >= 5, "the top pass of a multi-pass transform");
     constexpr int H = G::R / 2;
     for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
@@ -52,10 +50,10 @@ __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __
     }
 }
 
-template <int SET, int M, int C>
+template <int SET, int M, int C, int MR>
 __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
-    constexpr int NP = sch_np(M);
+    constexpr int NP = sch_np(M, MR);
     static_assert(NP >= 2, "column transforms have at least two passes");
     const ProdPtrs P = select_product(args, batch);
     // grid.y: prime*2 + operand, or just the prime for a square (one operand)
@@ -80,16 +78,16 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
         stage_rows<M, C>(sm, dig, N2, c0, nd, 0, 1 << (M - 1));
         cp_async_wait<0>();
         __syncthreads();
-        col_top_upper_zero<SET, M, C>(sm, tw, pc);
+        col_top_upper_zero<SET, M, C, MR>(sm, tw, pc);
     } else {
         stage_cols<M, C>(sm, dig, N2, c0, nd);
         __syncthreads();
-        col_pass<SET, M, 0, false, C, true>(sm, tw, pc);
+        col_pass<SET, M, 0, false, C, true, MR>(sm, tw, pc);
     }
     __syncthreads();
-    col_passes<SET, M, 1, NP - 2, false, C>(sm, tw, pc);
+    col_passes<SET, M, 1, NP - 2, false, C, MR>(sm, tw, pc);
     {   // bottom pass (bits 0..4) with the four-step twiddle, straight to HBM
-        using G = Geom<M, NP - 1>;
+        using G = Geom<M, NP - 1, MR>;
         static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
         uint32_t* __restrict__ dst = P.work + ((uint64_t)(prime * 2 + operand) << args.k);
         for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
@@ -99,7 +97,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
             uint32_t x[1][32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
-            regs_pass<SET, M, NP - 1, false, 1>(x, u, tw, pc);
+            regs_pass<SET, M, NP - 1, false, 1, MR>(x, u, tw, pc);
             // slot 32u + q holds k1 = brev5(q) << (M-5) | brev(u): the twiddle
             // w^(i2*k1) is t * g^brev5(q) with t = w^(i2*brev(u)), g = w^(i2 << (M-5))
             const uint32_t i2 = c0 + col;
@@ -117,10 +115,10 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     }
 }
 
-template <int SET, int M, int C>
+template <int SET, int M, int C, int MR>
 __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
-    constexpr int NP = sch_np(M);
+    constexpr int NP = sch_np(M, MR);
     static_assert(NP >= 2, "column transforms have at least two passes");
     const ProdPtrs P = select_product(args, batch);
     const int prime = args.prime0 + blockIdx.y;
@@ -132,9 +130,9 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
     // the column tile, staged by 16-byte asynchronous copies
     stage_cols<M, C>(sm, wk, N2, c0, ~0ull);
     __syncthreads();
-    col_passes<SET, M, NP - 1, 1, true, C>(sm, tw, pc);
+    col_passes<SET, M, NP - 1, 1, true, C, MR>(sm, tw, pc);
     {   // top DIT pass: natural row order i1, straight to HBM
-        using G = Geom<M, 0>;
+        using G = Geom<M, 0, MR>;
         for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
             const int col = w & (C - 1);
             const uint32_t u = w / C;
@@ -142,7 +140,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
             uint32_t x[1][G::R];
 #pragma unroll
             for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS * C];
-            regs_pass<SET, M, 0, true, 1>(x, u, tw, pc);
+            regs_pass<SET, M, 0, true, 1, MR>(x, u, tw, pc);
             const uint32_t base = G::base(u);
 #pragma unroll
             for (int q = 0; q < G::R; ++q)
@@ -153,46 +151,12 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
 
 // ---------------------------------------------------------------------------
 
-// columns per CTA: 8 (32-byte sectors) while that fits three CTAs per SM
-static int col_group(int set, int m) { return (set == 1 && m >= 12) ? 4 : kColGroup; }
+#define PREC_COLS_CONFIGS(X)                                                                            \
+    X(0, 6, 4, 6) X(0, 6, 8, 6) X(0, 7, 4, 6) X(0, 7, 8, 6) X(0, 8, 4, 6) X(0, 8, 8, 6) X(0, 9, 4, 6)     \
+    X(0, 9, 8, 6) X(0, 10, 4, 4) X(0, 10, 8, 4) X(0, 10, 4, 6) X(0, 10, 8, 6) X(0, 11, 4, 4)              \
+    X(0, 11, 8, 4) X(0, 11, 4, 6) X(0, 11, 8, 6) X(1, 11, 4, 4) X(1, 11, 8, 4) X(1, 11, 4, 6)             \
+    X(1, 11, 8, 6) X(1, 12, 4, 6) X(1, 13, 4, 6)
 
-static size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
-
-#define PREC_COLS_SET0(X)                                                                        \
-    X(0, 6, kColGroup) X(0, 7, kColGroup) X(0, 8, kColGroup) X(0, 9, kColGroup) X(0, 10, kColGroup) \
-    X(0, 11, kColGroup)
-#define PREC_COLS_SET1(X) X(1, 11, kColGroup) X(1, 12, 4) X(1, 13, 4)
-
-void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
-    const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, (a.square ? 1 : 2) * nprimes, count);
-    const size_t smem = col_smem(m, cg);
-#define X(S, MM, CC) \
-    if (set == S && m == MM) { k_fwd_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }
-    PREC_COLS_SET0(X) PREC_COLS_SET1(X)
-#undef X
-}
-
-void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
-    const int m = a.k1, cg = col_group(set, m);
-    const dim3 grid((1u << a.k2) / cg, nprimes, count);
-    const size_t smem = col_smem(m, cg);
-#define X(S, MM, CC) \
-    if (set == S && m == MM) { k_inv_cols<S, MM, CC><<<grid, 256, smem, st>>>(a, batch); return; }
-    PREC_COLS_SET0(X) PREC_COLS_SET1(X)
-#undef X
-}
-
-int configure_cols() {
-    cudaError_t e = cudaSuccess;
-#define X(S, MM, CC)                                                                                    \
-    if (!e) e = cudaFuncSetAttribute(k_fwd_cols<S, MM, CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                     (int)col_smem(MM, CC));                                            \
-    if (!e) e = cudaFuncSetAttribute(k_inv_cols<S, MM, CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                     (int)col_smem(MM, CC));
-    PREC_COLS_SET0(X) PREC_COLS_SET1(X)
-#undef X
-    return (int)e;
-}
+inline size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
 
 }  // namespace precgpu

@@ -1,0 +1,31 @@
+// ntt_cols_fwd.cu -- instantiations and launcher of the forward column
+// kernel (k_fwd_cols, ntt_cols.cuh).
+#include "ntt_cols.cuh"
+
+namespace precgpu {
+
+void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
+    int cg, mr;
+    col_config(set, a.k1, a.cg, a.cmr, cg, mr);
+    const dim3 grid((1u << a.k2) / cg, (a.square ? 1 : 2) * nprimes, count);
+    const size_t smem = col_smem(a.k1, cg);
+#define X(S, MM, CC, RR)                                                     \
+    if (set == S && a.k1 == MM && cg == CC && mr == RR) {                     \
+        k_fwd_cols<S, MM, CC, RR><<<grid, 256, smem, st>>>(a, batch);         \
+        return;                                                             \
+    }
+    PREC_COLS_CONFIGS(X)
+#undef X
+}
+
+int configure_fwd_cols() {
+    cudaError_t e = cudaSuccess;
+#define X(S, MM, CC, RR)                                                                                   \
+    if (!e) e = cudaFuncSetAttribute(k_fwd_cols<S, MM, CC, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)col_smem(MM, CC));
+    PREC_COLS_CONFIGS(X)
+#undef X
+    return (int)e;
+}
+
+}  // namespace precgpu

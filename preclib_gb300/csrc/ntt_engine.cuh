@@ -38,26 +38,30 @@ constexpr int kPassUnroll = PREC_PASS_UNROLL;
 #ifndef PREC_SCH_MAXRB
 #define PREC_SCH_MAXRB 4
 #endif
-// passes above the bottom one cover at most PREC_SCH_MAXRB bits each
-__host__ __device__ constexpr int sch_np(int m) {
-    return m <= 5 ? 1 : 1 + (m - 5 + PREC_SCH_MAXRB - 1) / PREC_SCH_MAXRB;
+// passes above the bottom one cover at most mr bits each (the radix cap;
+// PREC_SCH_MAXRB is the default of the translation unit)
+__host__ __device__ constexpr int sch_np(int m, int mr = PREC_SCH_MAXRB) {
+    return m <= 5 ? 1 : 1 + (m - 5 + mr - 1) / mr;
 }
-__host__ __device__ constexpr int sch_rb(int m, int t) {
+__host__ __device__ constexpr int sch_rb(int m, int t, int mr = PREC_SCH_MAXRB) {
     return m <= 5 ? m
-                  : (t == sch_np(m) - 1 ? 5
-                                        : (m - 5) / (sch_np(m) - 1) + (t < (m - 5) % (sch_np(m) - 1) ? 1 : 0));
+                  : (t == sch_np(m, mr) - 1
+                         ? 5
+                         : (m - 5) / (sch_np(m, mr) - 1) + (t < (m - 5) % (sch_np(m, mr) - 1) ? 1 : 0));
 }
-__host__ __device__ constexpr int sch_lo(int m, int t) { return t < 0 ? m : sch_lo(m, t - 1) - sch_rb(m, t); }
+__host__ __device__ constexpr int sch_lo(int m, int t, int mr = PREC_SCH_MAXRB) {
+    return t < 0 ? m : sch_lo(m, t - 1, mr) - sch_rb(m, t, mr);
+}
 
 __host__ __device__ constexpr int padded(int n) { return n + (n >> 5); }
 
 // words per array in shared memory (== 4 mod 8)
 __host__ __device__ constexpr int astride_for(int m) { return ((padded(1 << m) + 7) & ~7) + 4; }
 
-template <int M, int T>
+template <int M, int T, int MR = PREC_SCH_MAXRB>
 struct Geom {
-    static constexpr int RB = sch_rb(M, T);
-    static constexpr int LO = sch_lo(M, T);
+    static constexpr int RB = sch_rb(M, T, MR);
+    static constexpr int LO = sch_lo(M, T, MR);
     static constexpr int R = 1 << RB;
     static constexpr int LGI = M - RB;  // log2 of items per array
     static constexpr uint32_t LOMASK = (1u << LO) - 1;
@@ -156,10 +160,10 @@ __device__ __forceinline__ void dit_regs(uint32_t (&x)[NA][1 << RB], uint32_t ul
     }
 }
 
-template <int SET, int M, int T, bool DIT, int NA>
-__device__ __forceinline__ void regs_pass(uint32_t (&x)[NA][Geom<M, T>::R], uint32_t u, const uint2* __restrict__ tw,
-                                          const PrimeC& c) {
-    using G = Geom<M, T>;
+template <int SET, int M, int T, bool DIT, int NA, int MR = PREC_SCH_MAXRB>
+__device__ __forceinline__ void regs_pass(uint32_t (&x)[NA][Geom<M, T, MR>::R], uint32_t u,
+                                          const uint2* __restrict__ tw, const PrimeC& c) {
+    using G = Geom<M, T, MR>;
     if constexpr (DIT) dit_regs<SET, G::LO, G::RB, NA>(x, u & G::LOMASK, tw, c);
     else dif_regs<SET, G::LO, G::RB, NA>(x, u & G::LOMASK, tw, c);
 }
@@ -251,10 +255,10 @@ __device__ __forceinline__ void stage_cols(uint32_t* sm, const uint32_t* __restr
 // P(i)*C + c; lanes cover C adjacent columns (twiddle loads broadcast).
 // DIGIT: the values are raw 32-bit digits, reduced on load.  Items
 // [w0, w1) of the pass (w1 < 0: all C << LGI items).
-template <int SET, int M, int T, bool DIT, int C, bool DIGIT = false>
+template <int SET, int M, int T, bool DIT, int C, bool DIGIT = false, int MR = PREC_SCH_MAXRB>
 __device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c, int w0 = 0,
                                          int w1 = -1) {
-    using G = Geom<M, T>;
+    using G = Geom<M, T, MR>;
     const int total = w1 < 0 ? (C << G::LGI) : w1;
 #pragma unroll kPassUnroll
     for (int w = w0 + threadIdx.x; w < total; w += blockDim.x) {
@@ -264,7 +268,7 @@ __device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__
         uint32_t x[1][G::R];
 #pragma unroll
         for (int q = 0; q < G::R; ++q) x[0][q] = DIGIT ? Ar<SET>::digit(s[q * G::QS * C], c) : s[q * G::QS * C];
-        regs_pass<SET, M, T, DIT, 1>(x, u, tw, c);
+        regs_pass<SET, M, T, DIT, 1, MR>(x, u, tw, c);
 #pragma unroll
         for (int q = 0; q < G::R; ++q) s[q * G::QS * C] = x[0][q];
     }
@@ -281,12 +285,12 @@ __device__ __forceinline__ void row_passes(uint32_t* sm, int astride, int narr, 
     }
 }
 
-template <int SET, int M, int T, int TEND, bool DIT, int C>
+template <int SET, int M, int T, int TEND, bool DIT, int C, int MR = PREC_SCH_MAXRB>
 __device__ __forceinline__ void col_passes(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
     if constexpr (DIT ? (T >= TEND) : (T <= TEND)) {
-        col_pass<SET, M, T, DIT, C>(sm, tw, c);
+        col_pass<SET, M, T, DIT, C, false, MR>(sm, tw, c);
         __syncthreads();
-        col_passes<SET, M, DIT ? T - 1 : T + 1, TEND, DIT, C>(sm, tw, c);
+        col_passes<SET, M, DIT ? T - 1 : T + 1, TEND, DIT, C, MR>(sm, tw, c);
     }
 }
 

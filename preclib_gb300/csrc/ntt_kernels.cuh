@@ -41,6 +41,8 @@ struct ProdArgs {
     int rows;           // rows per CTA of the row pass
     int square;         // a == b: one operand transform, pointwise square
     int prime0;         // first prime of this launch of the transform kernels (grid.y covers the rest)
+    int cg;             // columns per column-pass CTA (0: default)
+    int cmr;            // column pass radix cap, 4 or 6 (0: default)
     int pad;
     CrtConst crt;
     FieldArgs f;
@@ -144,7 +146,18 @@ void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
                      int nprimes = kPrimes);
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
                       int max_nblk = 0);
-int configure_cols();
+int configure_fwd_cols();
+int configure_inv_cols();
+
+// Column-pass configuration instantiated for (set, m = log2 N1) closest to
+// the requested columns per CTA and radix cap (0 = default: 8 columns,
+// radix cap 6).  The radix cap only changes the schedule of 2^10- and
+// 2^11-point columns; set 1's 2^12- and 2^13-point columns take 4 columns.
+inline void col_config(int set, int m, int req_cg, int req_mr, int& cg, int& mr) {
+    cg = (req_cg == 4 || req_cg == 8) ? req_cg : kColGroup;
+    if (set == 1 && m >= 12) cg = 4;
+    mr = (m == 10 || m == 11) && req_mr == 4 ? 4 : 6;
+}
 int configure_rows();
 int configure_small();
 

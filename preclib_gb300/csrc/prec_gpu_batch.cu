@@ -117,6 +117,8 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
             args.k1 = c.pl.k1;
             args.k2 = c.pl.k2;
             args.rows = c.pl.rows;
+            args.cg = c.pl.cg;
+            args.cmr = c.pl.cmr;
             args.square = c.square;
             args.crt = c.pl.crt;
             args.f = ctx_field(c.pl.set);

@@ -112,11 +112,7 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
         return 0;
     }
     pl.path = 1;
-    // column length N1 = 2^k1, row length N2 = 2^k2; set 1 keeps the rows
-    // at 2^13 so its column CTAs stay within a third of shared memory
-    pl.k1 = pl.set == 0 ? k / 2 : k - 13;
-    pl.k2 = k - pl.k1;
-    ntt_row_threads(pl.k2, 1 << pl.k1, &pl.rows);
+    apply_config(pl, tuned_config(k));
     const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
     pl.nblk = (int)((lout + bl - 1) / bl);
     pl.work_bytes = ((size_t)2 * kPrimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
@@ -146,7 +142,6 @@ struct Ctx {
 };
 
 static Ctx g_ctx;
-constexpr int kSplitMinLog2 = 19;  // smallest transform run as per-prime stream chains
 static thread_local prec_gpu_stats_t t_stats;
 
 int cuda_code(cudaError_t e) {
@@ -263,6 +258,10 @@ static int init_locked(Ctx& c, int device) {
     if (r) return r;
     CK(cudaDeviceSynchronize());
     c.ready = true;
+    // a saved tuning table (an invalid file leaves the defaults in place)
+    if (const char* tf = std::getenv("PREC_GPU_TUNE_FILE")) {
+        if (prec_gpu_tune_load(tf) != PREC_GPU_OK) std::fprintf(stderr, "prec_gpu: ignoring tuning table %s\n", tf);
+    }
     return 0;
 }
 
@@ -343,17 +342,24 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.k2 = pl.k2;
         args.nblk = pl.nblk;
         args.rows = pl.rows;
+        args.cg = pl.cg;
+        args.cmr = pl.cmr;
         args.square = square;
         args.crt = pl.crt;
         args.f = c.field[pl.set];
-        // per-prime chains from 2^19 points up (below, the extra launches cost
-        // more than the overlapped tail waves save)
-        const bool split = c.split_primes && pl.k >= kSplitMinLog2;
+        const bool split = c.split_primes && pl.split;
         ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr);
     }
     CK(cudaGetLastError());
     return 0;
 }
+
+int ctx_enqueue_ntt_locked(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
+                           const Plan& pl, cudaStream_t st) {
+    return enqueue_ntt(g_ctx, d_a, la, d_b, lb, d_out, pl, st);
+}
+
+int ctx_ensure_ws_locked(size_t bytes) { return ensure_ws(g_ctx, bytes); }
 
 static size_t trim(const uint64_t* a, size_t n) {
     while (n > 0 && a[n - 1] == 0) --n;

@@ -19,12 +19,40 @@ struct Plan {
     int path = 0;  // 0 single CTA, 1 four-step
     int nblk = 0;
     int rows = 0;  // rows per CTA of the row pass
+    int cg = 0;    // columns per column-pass CTA (0: default)
+    int cmr = 0;   // column pass radix cap (0: default)
+    int split = 0; // per-prime stream chains for a single product
     CrtConst crt{};
     size_t work_bytes = 0;  // work buffer + carry words of the four-step path
 };
 
-// da, db: 32-bit digit counts (upper bounds are fine); lout = La + Lb
+// da, db: 32-bit digit counts (upper bounds are fine); lout = La + Lb.
+// The four-step kernel configuration comes from the tuning table (the
+// autotuner's choice for the length, else the default configuration).
 int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl);
+
+// Kernel configuration of one four-step transform length (the autotuner's
+// unit; prec_gpu_tune.cu).
+struct KernelConfig {
+    int k1 = 0;     // log2 column length (row length 2^(k - k1))
+    int cg = 0;     // columns per column-pass CTA: 4 or 8
+    int cmr = 0;    // column pass radix cap: 4 or 6
+    int rows = 0;   // rows per row-pass CTA
+    int split = 0;  // per-prime stream chains
+};
+KernelConfig default_config(int k);
+bool config_valid(int k, const KernelConfig& c);
+// the table's configuration for length 2^k (k >= 13)
+KernelConfig tuned_config(int k);
+// fills the four-step fields of a plan from a configuration
+void apply_config(Plan& pl, const KernelConfig& c);
+
+// Enqueues one NTT-band product with plan `pl` on device pointers (the
+// library workspace must hold pl.work_bytes: ctx_ensure_ws_locked).  Call
+// with the context lock held.
+int ctx_enqueue_ntt_locked(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
+                           const Plan& pl, cudaStream_t st);
+int ctx_ensure_ws_locked(size_t bytes);
 
 // the process-wide context: its lock, initialisation (idempotent, call
 // with the lock held), prime-set tables and device error word

@@ -117,6 +117,8 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         args.k2 = r.pl.k2;
         args.nblk = r.pl.nblk;
         args.rows = r.pl.rows;
+        args.cg = r.pl.cg;
+        args.cmr = r.pl.cmr;
         args.crt = r.pl.crt;
         args.f = ctx_field(r.pl.set);
         ntt_launch_4step(r.pl.set, args, st);

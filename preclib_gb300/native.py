@@ -26,7 +26,8 @@ EXPORTS = (
     "prec_gpu_fft_digit_bits", "prec_gpu_batch_create", "prec_gpu_batch_run", "prec_gpu_batch_info",
     "prec_gpu_batch_destroy", "prec_gpu_mul_batch", "prec_gpu_serve_create", "prec_gpu_serve_submit",
     "prec_gpu_serve_wait", "prec_gpu_serve_drain", "prec_gpu_serve_stats", "prec_gpu_serve_destroy",
-    "prec_gpu_sqr",
+    "prec_gpu_sqr", "prec_gpu_autotune", "prec_gpu_tune_get", "prec_gpu_tune_set", "prec_gpu_tune_reset",
+    "prec_gpu_tune_save", "prec_gpu_tune_load",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -42,6 +43,16 @@ class Product(ctypes.Structure):
     """prec_gpu_product_t: device pointers and limb counts of one product."""
     _fields_ = [("a", ctypes.c_void_p), ("an", ctypes.c_size_t), ("b", ctypes.c_void_p),
                 ("bn", ctypes.c_size_t), ("out", ctypes.c_void_p)]
+
+
+class TuneEntry(ctypes.Structure):
+    """prec_gpu_tune_entry_t: kernel configuration of one NTT length."""
+    _fields_ = [("log2_n", ctypes.c_int), ("log2_cols", ctypes.c_int), ("col_group", ctypes.c_int),
+                ("col_radix_cap", ctypes.c_int), ("rows_per_cta", ctypes.c_int), ("split_primes", ctypes.c_int),
+                ("ms", ctypes.c_float), ("default_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class ServeStats(ctypes.Structure):
@@ -77,6 +88,19 @@ def lib() -> ctypes.CDLL:
             f.restype = ctypes.c_int
         L.prec_gpu_sqr.argtypes = [_u64p, ctypes.c_size_t, _u64p]
         L.prec_gpu_sqr.restype = ctypes.c_int
+        L.prec_gpu_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneEntry), ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t)]
+        L.prec_gpu_autotune.restype = ctypes.c_int
+        L.prec_gpu_tune_get.argtypes = [ctypes.c_int, ctypes.POINTER(TuneEntry)]
+        L.prec_gpu_tune_get.restype = ctypes.c_int
+        L.prec_gpu_tune_set.argtypes = [ctypes.POINTER(TuneEntry)]
+        L.prec_gpu_tune_set.restype = ctypes.c_int
+        L.prec_gpu_tune_reset.argtypes = []
+        L.prec_gpu_tune_reset.restype = ctypes.c_int
+        L.prec_gpu_tune_save.argtypes = [ctypes.c_char_p]
+        L.prec_gpu_tune_save.restype = ctypes.c_int
+        L.prec_gpu_tune_load.argtypes = [ctypes.c_char_p]
+        L.prec_gpu_tune_load.restype = ctypes.c_int
         L.prec_gpu_mul_device.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                           ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         L.prec_gpu_mul_device.restype = ctypes.c_int
@@ -170,6 +194,40 @@ def sqr(a) -> np.ndarray:
     out = np.empty(max(2 * len(a), 1), dtype=np.uint64)
     check(lib().prec_gpu_sqr(_p(a), len(a), _p(out)), "prec_gpu_sqr")
     return out[: 2 * len(a)]
+
+
+def autotune(kmin: int = 13, kmax: int = 26):
+    """Tunes the kernel configuration of NTT lengths 2^kmin .. 2^kmax on the
+    current device; returns one dict per length (chosen config and times)."""
+    cap = 32
+    arr = (TuneEntry * cap)()
+    n = ctypes.c_size_t(0)
+    check(lib().prec_gpu_autotune(kmin, kmax, arr, cap, ctypes.byref(n)), "prec_gpu_autotune")
+    return [arr[i].as_dict() for i in range(min(n.value, cap))]
+
+
+def tune_get(log2_n: int) -> dict:
+    e = TuneEntry()
+    check(lib().prec_gpu_tune_get(log2_n, ctypes.byref(e)), "prec_gpu_tune_get")
+    return e.as_dict()
+
+
+def tune_set(**cfg) -> None:
+    """Installs a configuration: keys of TuneEntry (log2_n required)."""
+    e = TuneEntry(**{k: v for k, v in cfg.items() if k in dict(TuneEntry._fields_)})
+    check(lib().prec_gpu_tune_set(ctypes.byref(e)), "prec_gpu_tune_set")
+
+
+def tune_reset() -> None:
+    check(lib().prec_gpu_tune_reset(), "prec_gpu_tune_reset")
+
+
+def tune_save(path: str) -> None:
+    check(lib().prec_gpu_tune_save(path.encode()), "prec_gpu_tune_save")
+
+
+def tune_load(path: str) -> None:
+    check(lib().prec_gpu_tune_load(path.encode()), "prec_gpu_tune_load")
 
 
 def mul_device(a_ptr: int, an: int, b_ptr: int, bn: int, out_ptr: int, stream: int = 0) -> None:

@@ -103,3 +103,31 @@ def test_batch_one_shot_and_chunking(gpu, monkeypatch):
     gpu.mul_batch(db.items(), torch.cuda.current_stream().cuda_stream)
     for i in range(len(sizes)):
         assert np.array_equal(db.result(i), _plain(gpu, torch, db, i)), (i, sizes[i])
+
+
+def test_config3_workload_tuned_vs_oracle(gpu):
+    """The batch benchmark's workload (4096 products, lo log-uniform in
+    [200, 65536] limbs, hi = lo * U[1, 2], SplitMix64 seed 7) after the
+    autotuner picked its length classes' kernels: a seeded sample of 64
+    products equals the oracle, and every product equals the plain path."""
+    torch = pytest.importorskip("torch")
+    from preclib_gb300 import workloads
+    lo, hi = workloads.batch_sizes(7, 4096)
+    sizes = [(int(h), int(l)) for l, h in zip(lo, hi)]
+    try:
+        gpu.autotune(13, max(gpu.ntt_log2(a, b) for a, b in sizes))
+        db = DevBatch(torch, sizes, 7)
+        b = gpu.Batch(db.items())
+        b.run()
+        gpu.stream_check()
+        b.close()
+        rng = np.random.default_rng(7)
+        for i in sorted(rng.choice(len(sizes), size=64, replace=False).tolist()):
+            a_, b_ = db.operands(i)
+            assert np.array_equal(db.result(i), O.mul_ntt(a_, b_)), sizes[i]
+        out = db.out.cpu().numpy().view(np.uint64)
+        for i in range(0, len(sizes), 97):
+            o, (a_, b_) = db.off[i], sizes[i]
+            assert np.array_equal(out[o:o + a_ + b_], _plain(gpu, torch, db, i)), sizes[i]
+    finally:
+        gpu.tune_reset()

@@ -5,6 +5,7 @@
 # nothing and exits 0 when it is absent.  Outputs go only to oracle/_ref/.
 #   libprecref.so       portable build (-O3, no SIMD flags), COUNT_FFTS on
 #   libprecref_avx2.so  x86-64 only: -mavx2 build, for the CPU-baseline table
+#   pi_ref              (argument "pi") preclib's pi program, for golden hashes
 #   interposed/         (argument "interposed") preclib's fft_torture,
 #                       test_opt_smoke and pi_chudnovsky linked with the GPU
 #                       mul_ntt / mul_fft instead of src/mul_ntt.cpp, mul_fft.cpp
@@ -17,6 +18,12 @@ if [ ! -f "$REF/prec.hpp" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
+if [ "${1:-}" = "pi" ]; then
+  # preclib's own pi program (its CPU multiply), for the golden digit hashes
+  "${CXX:-g++}" -O3 -std=c++17 -I"$REF" "$REF/pi/pi_chudnovsky.cpp" "$REF"/src/*.cpp -o "$OUT/pi_ref.tmp"
+  mv "$OUT/pi_ref.tmp" "$OUT/pi_ref"
+  exit 0
+fi
 if [ "${1:-}" = "interposed" ]; then
   # preclib's own programs with mul_ntt/mul_fft from the GPU library
   # (needs preclib_gb300/lib/libprecgpu.so built first)

@@ -59,8 +59,26 @@ def build(verbose: bool = False, extra=()) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, out)
+    build_pi()
     if verbose:
         print("built", out)
+    return out
+
+
+PI_SOURCES = ("bignum.cpp", "pi_chudnovsky.cpp")
+PI_EXE = "pi_gb300"
+
+
+def build_pi() -> str:
+    """The pi program (pi/*.cpp, host C++) linked against lib/libprecgpu.so."""
+    srcs = [os.path.join(PKG, "pi", f) for f in PI_SOURCES]
+    out = os.path.join(LIBDIR, PI_EXE)
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-pthread", "-I", os.path.join(PKG, "..", "include"),
+           *srcs, "-L", LIBDIR, "-lprecgpu", "-Xlinker", "-rpath=" + LIBDIR, "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("pi program build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(out + ".tmp", out)
     return out
 
 

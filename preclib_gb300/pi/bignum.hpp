@@ -1,0 +1,79 @@
+// bignum.hpp -- natural numbers for the pi program: host-side linear
+// arithmetic (add, subtract, shift, compare, single-limb multiply and
+// divide) and the Newton-based operations built on a multiply backend
+// (reciprocal, exact division, integer square root, decimal conversion).
+//
+// Every product above the backend's host threshold goes to the backend;
+// the pi program's backend is the GPU library (pi_gpu.cpp), and many
+// independent products of one step (a binary-splitting level, a level of
+// the decimal conversion) are handed over together as one batch.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <string>
+#include <vector>
+
+namespace precpi {
+
+using u64 = uint64_t;
+using u128 = unsigned __int128;
+
+// little-endian limbs, no zero top limb (zero = empty)
+struct Nat {
+    std::vector<u64> d;
+    Nat() = default;
+    explicit Nat(u64 v) {
+        if (v) d.push_back(v);
+    }
+    bool zero() const { return d.empty(); }
+    size_t size() const { return d.size(); }
+};
+
+// Products: one at a time or many independent ones (the batch form).
+struct MulBackend {
+    virtual ~MulBackend() = default;
+    // out = a * b (a or b may be zero); a and b may be the same object
+    virtual void mul(const Nat& a, const Nat& b, Nat& out) = 0;
+    // out[i] = *a[i] * *b[i]
+    virtual void mul_many(const std::vector<const Nat*>& a, const std::vector<const Nat*>& b,
+                          std::vector<Nat>& out) = 0;
+};
+
+void set_backend(MulBackend* be);
+MulBackend& backend();
+
+// host threads for the linear work (and small products)
+void parallel_for(size_t n, const std::function<void(size_t)>& fn);
+
+void normalize(Nat& x);
+int cmp(const Nat& a, const Nat& b);
+size_t bitlen(const Nat& a);
+Nat add(const Nat& a, const Nat& b);
+Nat sub(const Nat& a, const Nat& b);  // a >= b
+void add_in(Nat& a, const Nat& b);    // a += b
+void sub_in(Nat& a, const Nat& b);    // a -= b, a >= b
+Nat shl(const Nat& a, size_t bits);
+Nat shr(const Nat& a, size_t bits);
+Nat pow2(size_t bits);
+Nat mul_u64(const Nat& a, u64 b);
+u64 divmod_u64(Nat& a, u64 b);  // a /= b, returns a mod b
+// schoolbook product on the host (small operands)
+void mul_school(const u64* a, size_t an, const u64* b, size_t bn, u64* out);
+
+Nat mul(const Nat& a, const Nat& b);
+Nat sqr(const Nat& a);
+Nat pow_u64(u64 base, size_t e);
+
+// Reciprocal: X with |X - 2^(bitlen(D) + p) / D| <= 4, p >= 1.
+Nat recip(const Nat& D, size_t p);
+// exact floor division and remainder (D > 0)
+void divmod(const Nat& N, const Nat& D, Nat& q, Nat& r);
+// floor(sqrt(n))
+Nat isqrt(const Nat& n);
+
+// Exact decimal digits of x, padded with leading zeros to at least
+// `width` characters.
+std::string to_decimal(const Nat& x, size_t width);
+
+}  // namespace precpi

@@ -1,0 +1,352 @@
+// pi_chudnovsky.cpp -- pi by the Chudnovsky series on the GB300 multiply.
+//
+//   pi_gb300 DIGITS [--phases] [--full] [--file PATH]
+//
+// Same computation and output as preclib's pi/pi_chudnovsky.cpp (same
+// guard digits, term count, scaled square root, floor divisions, decimal
+// text and file format: "3.<DIGITS digits>\n"), so the digits are
+// byte-identical.  What differs is the order of work:
+//   * binary splitting runs level by level over the whole term range
+//     instead of depth first (pi_chudnovsky.cpp:117-148): every level's
+//     products (Q = Ql*Qr, T terms Tl*Qr and Tr*Pl, P = Pl*Pr where a later
+//     level needs it) are independent and go to the GPU as one batch
+//     (prec_gpu_mul_batch); the node values are shape independent
+//     (T(a,b) = sum_k t_k P(a,k) Q(k+1,b)), so any tree gives the same Q, T;
+//   * the square root, the final division and the decimal conversion run
+//     Newton iterations whose products go to the GPU (bignum.cpp), the
+//     conversion's splits once more as one batch per level.
+// Products of at most kHostMaxLimbs limbs (the tree's lowest levels) run
+// on the host, as the reference multiplies them with its schoolbook and
+// Karatsuba code; everything larger is computed by libprecgpu.  There is
+// no CPU path for those: without a device the program stops.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/prec_gpu.h"
+#include "bignum.hpp"
+
+using namespace precpi;
+
+namespace {
+
+constexpr u64 kC3Over24 = 10939058860032000ull;  // 640320^3 / 24
+constexpr u64 kA = 13591409ull;
+constexpr u64 kB = 545140134ull;
+constexpr size_t kHostMaxLimbs = 32;  // products up to this size stay on the host
+
+double now_sec() {
+    static const auto t0 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+[[noreturn]] void die(const char* what, int rc) {
+    std::fprintf(stderr, "pi_gb300: %s: %s\n", what, prec_gpu_strerror(rc));
+    std::exit(1);
+}
+
+void check_cuda(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "pi_gb300: %s: %s\n", what, cudaGetErrorString(e));
+        std::exit(1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// multiply backend on libprecgpu
+// ---------------------------------------------------------------------------
+
+struct GpuBackend : MulBackend {
+    cudaStream_t st = nullptr;
+    u64* h_buf = nullptr;  // pinned staging of a batch (operands, then results)
+    size_t h_cap = 0;
+    u64* d_buf = nullptr;  // device copy of the same layout
+    size_t d_cap = 0;
+    size_t gpu_products = 0, host_products = 0, batches = 0;
+
+    GpuBackend() { check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream"); }
+    ~GpuBackend() override {
+        if (h_buf) cudaFreeHost(h_buf);
+        if (d_buf) cudaFree(d_buf);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    static bool small(const Nat& a, const Nat& b) { return std::max(a.size(), b.size()) <= kHostMaxLimbs; }
+
+    void mul(const Nat& a, const Nat& b, Nat& out) override {
+        out.d.assign(a.size() + b.size(), 0);
+        if (small(a, b)) {
+            mul_school(a.d.data(), a.size(), b.d.data(), b.size(), out.d.data());
+            ++host_products;
+        } else {
+            const int rc = prec_gpu_mul(a.d.data(), a.size(), b.d.data(), b.size(), out.d.data());
+            if (rc) die("prec_gpu_mul", rc);
+            ++gpu_products;
+        }
+        normalize(out);
+    }
+
+    void reserve(size_t limbs) {
+        if (limbs > h_cap) {
+            if (h_buf) cudaFreeHost(h_buf);
+            h_cap = limbs + limbs / 4;
+            check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&h_buf), h_cap * sizeof(u64), 0), "pinned buffer");
+        }
+        if (limbs > d_cap) {
+            if (d_buf) cudaFree(d_buf);
+            d_cap = limbs + limbs / 4;
+            check_cuda(cudaMalloc(reinterpret_cast<void**>(&d_buf), d_cap * sizeof(u64)), "device buffer");
+        }
+    }
+
+    static size_t up32(size_t x) { return (x + 31) & ~(size_t)31; }  // 256-byte aligned operands
+
+    void mul_many(const std::vector<const Nat*>& A, const std::vector<const Nat*>& B,
+                  std::vector<Nat>& out) override {
+        const size_t n = A.size();
+        out.assign(n, Nat());
+        std::vector<size_t> host, gpu;
+        for (size_t i = 0; i < n; ++i) {
+            if (A[i]->zero() || B[i]->zero()) continue;
+            (small(*A[i], *B[i]) ? host : gpu).push_back(i);
+        }
+        parallel_for(host.size(), [&](size_t u) {
+            const size_t i = host[u];
+            out[i].d.assign(A[i]->size() + B[i]->size(), 0);
+            mul_school(A[i]->d.data(), A[i]->size(), B[i]->d.data(), B[i]->size(), out[i].d.data());
+            normalize(out[i]);
+        });
+        host_products += host.size();
+        if (gpu.empty()) return;
+        // layout: each distinct operand once, then the results
+        std::unordered_map<const Nat*, size_t> where;
+        std::vector<const Nat*> uniq;
+        size_t in = 0;
+        for (size_t i : gpu)
+            for (const Nat* x : {A[i], B[i]})
+                if (where.emplace(x, in).second) {
+                    uniq.push_back(x);
+                    in += up32(x->size());
+                }
+        std::vector<size_t> ooff(gpu.size());
+        size_t total = in;
+        for (size_t u = 0; u < gpu.size(); ++u) {
+            ooff[u] = total;
+            total += up32(A[gpu[u]]->size() + B[gpu[u]]->size());
+        }
+        reserve(total);
+        parallel_for(uniq.size(), [&](size_t u) {
+            std::memcpy(h_buf + where[uniq[u]], uniq[u]->d.data(), uniq[u]->size() * sizeof(u64));
+        });
+        check_cuda(cudaMemcpyAsync(d_buf, h_buf, in * sizeof(u64), cudaMemcpyHostToDevice, st), "H2D");
+        std::vector<prec_gpu_product_t> items(gpu.size());
+        for (size_t u = 0; u < gpu.size(); ++u) {
+            const size_t i = gpu[u];
+            items[u].a = d_buf + where[A[i]];
+            items[u].an = A[i]->size();
+            items[u].b = d_buf + where[B[i]];
+            items[u].bn = B[i]->size();
+            items[u].out = d_buf + ooff[u];
+        }
+        const int rc = prec_gpu_mul_batch(items.data(), items.size(), st);
+        if (rc) die("prec_gpu_mul_batch", rc);
+        check_cuda(cudaMemcpyAsync(h_buf + in, d_buf + in, (total - in) * sizeof(u64), cudaMemcpyDeviceToHost, st),
+                   "D2H");
+        check_cuda(cudaStreamSynchronize(st), "batch");
+        parallel_for(gpu.size(), [&](size_t u) {
+            const size_t i = gpu[u];
+            const size_t len = A[i]->size() + B[i]->size();
+            out[i].d.assign(h_buf + ooff[u], h_buf + ooff[u] + len);
+            normalize(out[i]);
+        });
+        gpu_products += gpu.size();
+        ++batches;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// binary splitting, one level at a time
+// ---------------------------------------------------------------------------
+
+struct Node {
+    Nat p, q, t;
+    bool neg = false;  // sign of t
+};
+
+Nat from_u128(u128 v) {
+    Nat r;
+    r.d.push_back((u64)v);
+    r.d.push_back((u64)(v >> 64));
+    normalize(r);
+    return r;
+}
+
+// term k of the series (pi_chudnovsky.cpp:119-136)
+Node leaf(u64 k) {
+    Node n;
+    if (k == 0) {
+        n.p = Nat(1);
+        n.q = Nat(1);
+        n.t = Nat(kA);
+        return n;
+    }
+    const u128 p = (u128)(6 * k - 5) * (2 * k - 1) * (6 * k - 1);
+    const u128 q = (u128)k * k * k * kC3Over24;
+    const u128 t = p * (u128)(kB * k + kA);
+    n.p = from_u128(p);
+    n.q = from_u128(q);
+    n.t = from_u128(t);
+    n.neg = (k & 1) != 0;
+    return n;
+}
+
+// signed sum of two magnitudes
+void signed_add(Nat a, bool an, Nat b, bool bn, Nat& r, bool& rn) {
+    if (an == bn) {
+        add_in(a, b);
+        r = std::move(a);
+        rn = an && !r.zero();
+        return;
+    }
+    if (cmp(a, b) >= 0) {
+        sub_in(a, b);
+        r = std::move(a);
+        rn = an && !r.zero();
+    } else {
+        sub_in(b, a);
+        r = std::move(b);
+        rn = bn && !r.zero();
+    }
+}
+
+// Q(0, terms) and T(0, terms)
+void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
+    std::vector<Node> lv(terms);
+    parallel_for(terms, [&](size_t k) { lv[k] = leaf(k); });
+    while (lv.size() > 1) {
+        const size_t m = lv.size(), pairs = m / 2;
+        // the last node of a level (the range ending at `terms`) never needs P
+        const bool last_pair_is_last = (m % 2) == 0;
+        std::vector<const Nat*> A, B;
+        A.reserve(4 * pairs);
+        B.reserve(4 * pairs);
+        for (size_t i = 0; i < pairs; ++i) {
+            const Node& l = lv[2 * i];
+            const Node& r = lv[2 * i + 1];
+            A.push_back(&l.q), B.push_back(&r.q);  // Q
+            A.push_back(&l.t), B.push_back(&r.q);  // Tl * Qr
+            A.push_back(&r.t), B.push_back(&l.p);  // Tr * Pl
+            const bool need_p = !(last_pair_is_last && i == pairs - 1);
+            if (need_p) A.push_back(&l.p), B.push_back(&r.p);
+        }
+        std::vector<Nat> prod;
+        backend().mul_many(A, B, prod);
+        std::vector<size_t> base(pairs + 1, 0);
+        for (size_t i = 0; i < pairs; ++i) base[i + 1] = base[i] + (last_pair_is_last && i == pairs - 1 ? 3 : 4);
+        std::vector<Node> up((m + 1) / 2);
+        parallel_for(pairs, [&](size_t i) {
+            const size_t b = base[i];
+            Node& u = up[i];
+            u.q = std::move(prod[b]);
+            signed_add(std::move(prod[b + 1]), lv[2 * i].neg, std::move(prod[b + 2]), lv[2 * i + 1].neg, u.t,
+                       u.neg);
+            if (base[i + 1] - b == 4) u.p = std::move(prod[b + 3]);
+        });
+        if (m % 2) up.back() = std::move(lv.back());
+        lv.swap(up);
+    }
+    Q = std::move(lv[0].q);
+    T = std::move(lv[0].t);
+    tneg = lv[0].neg;
+}
+
+struct Phases {
+    double split = 0, sqrt = 0, div = 0, dec = 0;
+};
+
+// pi_chudnovsky.cpp:162-194
+std::string pi_digits(size_t digits, Phases& ph) {
+    const size_t guard = 10, work = digits + guard, terms = work / 14 + 2;
+    double t0 = now_sec();
+    Nat Q, T;
+    bool tneg = false;
+    binary_split(terms, Q, T, tneg);
+    double t1 = now_sec();
+    if (tneg || T.zero()) return "error";
+    const Nat n = mul_u64(pow_u64(10, 2 * work), 10005);
+    const Nat root = isqrt(n);
+    double t2 = now_sec();
+    const Nat num = mul(mul_u64(Q, 426880), root);
+    Nat pi, rem;
+    divmod(num, T, pi, rem);
+    divmod_u64(pi, 10000000000ull);
+    double t3 = now_sec();
+    std::string s = to_decimal(pi, 0);
+    double t4 = now_sec();
+    ph = Phases{t1 - t0, t2 - t1, t3 - t2, t4 - t3};
+    if (digits == 0) return s;
+    if (s.size() <= digits) s.insert(0, digits + 1 - s.size(), '0');
+    s.insert(s.end() - (long long)digits, '.');
+    return s;
+}
+
+std::string short_form(const std::string& s, bool full) {
+    if (full || s.size() <= 24) return s;
+    return s.substr(0, 11) + "..." + s.substr(s.size() - 10);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    size_t digits = 100;
+    bool phases = false, full = false;
+    std::string file;
+    if (argc > 1) digits = (size_t)std::strtoull(argv[1], nullptr, 10);
+    for (int i = 2; i < argc; ++i) {
+        const std::string a = argv[i];
+        if (a == "--phases") phases = true;
+        if (a == "--full") full = true;
+        if (a == "--file" && i + 1 < argc) file = argv[++i];
+    }
+    // k^3 * 640320^3/24 must fit 128 bits: k < 3.1e7, about 4.3e8 digits
+    if (digits > 400000000ull) {
+        std::fprintf(stderr, "pi_gb300: at most 400000000 digits\n");
+        return 1;
+    }
+    const int rc = prec_gpu_init(-1);
+    if (rc) die("prec_gpu_init", rc);
+    GpuBackend be;
+    set_backend(&be);
+    now_sec();
+    const double start = now_sec();
+    Phases ph;
+    const std::string out = pi_digits(digits, ph);
+    const double sec = now_sec() - start;
+    if (!file.empty()) {
+        std::ofstream f(file.c_str(), std::ios::out | std::ios::binary);
+        if (!f) {
+            std::fprintf(stderr, "pi_gb300: cannot open %s\n", file.c_str());
+            return 1;
+        }
+        f << out << "\n";
+    }
+    std::printf("%s\n", short_form(out, full).c_str());
+    if (phases) {
+        std::fprintf(stderr, "binary_split %.6f sec\n", ph.split);
+        std::fprintf(stderr, "sqrt_scale %.6f sec\n", ph.sqrt);
+        std::fprintf(stderr, "final_div %.6f sec\n", ph.div);
+        std::fprintf(stderr, "to_decimal %.6f sec\n", ph.dec);
+        std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu\n", be.gpu_products,
+                     be.host_products, be.batches);
+    }
+    if (!file.empty()) std::fprintf(stderr, "wrote %s\n", file.c_str());
+    std::fprintf(stderr, "time %.6f sec\n", sec);
+    return 0;
+}

@@ -1,0 +1,33 @@
+"""GPU parity of the pi program (preclib_gb300/pi): its output file is
+byte-identical to preclib's own pi program at 10^2 .. 10^7 digits (hashes
+generated from the reference by tests/golden/make_pi_golden.py)."""
+import hashlib
+import json
+import os
+import subprocess
+
+import pytest
+
+from preclib_gb300 import build as B
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EXE = os.path.join(B.LIBDIR, B.PI_EXE)
+
+
+def _runs():
+    with open(os.path.join(ROOT, "tests", "golden", "pi.json")) as f:
+        return {r["digits"]: r for r in json.load(f)["runs"]}
+
+
+@pytest.mark.parametrize("digits", [100, 1000, 10000, 100000, 1000000, 10000000])
+def test_pi_digits_match_reference(gpu, tmp_path, digits):
+    want = _runs()[digits]
+    out = tmp_path / "pi.txt"
+    r = subprocess.run([EXE, str(digits), "--phases", "--file", str(out)], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    data = out.read_bytes()
+    assert len(data) == want["bytes"]
+    assert hashlib.sha256(data).hexdigest() == want["sha256"]
+    assert data.startswith(b"3.14159265")

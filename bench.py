@@ -558,6 +558,53 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+PI_DIGITS = 100000000
+
+
+def run_pi(args):
+    """pi to 10^8 decimal digits (the Chudnovsky program, preclib_gb300/pi):
+    a step is one whole run of the program (binary splitting with one batch
+    per tree level, square root, division, decimal conversion); the output
+    file must be byte-identical to preclib's own pi program (SHA-256 of its
+    10^8-digit output, tests/golden/pi.json)."""
+    from preclib_gb300 import build as B
+    exe = os.path.join(B.LIBDIR, B.PI_EXE)
+    with open(os.path.join(ROOT, "tests", "golden", "pi.json")) as f:
+        want = {r["digits"]: r for r in json.load(f)["runs"]}[PI_DIGITS]
+    steps = max(1, min(args.steps, 3))
+    runs, exact = [], True
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "pi.txt")
+        for i in range(1 + steps):  # one untimed warm-up run
+            t = time.perf_counter()
+            r = subprocess.run([exe, str(PI_DIGITS), "--phases", "--file", out], capture_output=True, text=True)
+            wall = time.perf_counter() - t
+            if r.returncode != 0:
+                raise SystemExit("pi program failed: " + r.stderr[-500:])
+            data = open(out, "rb").read()
+            exact = exact and len(data) == want["bytes"] and hashlib.sha256(data).hexdigest() == want["sha256"]
+            ph = {}
+            for line in r.stderr.splitlines():
+                parts = line.split()
+                if len(parts) == 3 and parts[2] == "sec":
+                    ph[parts[0]] = float(parts[1])
+            if i:
+                runs.append((wall, ph))
+    wall = statistics.median(w for w, _ in runs)
+    phases = {k: round(statistics.median(p[k] for _, p in runs), 3) for k in runs[0][1]}
+    line = {
+        "metric": "pi 10^8 digits, whole program s", "value": round(wall, 3), "unit": "s", "n_gpus": 1,
+        "steps": steps, "warmup": 1, "ms_per_step": round(wall * 1e3, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "pi to 100,000,000 decimal digits by the Chudnovsky series",
+                   "l2": "n/a (whole program)"},
+        "phases_s": phases, "bit_exact": bool(exact),
+        "e2e": {"value": round(wall, 3), "unit": "s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_cast(addr, typ):
     import ctypes
     return ctypes.cast(ctypes.c_void_p(addr), typ)
@@ -569,9 +616,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="1m", choices=["1m", "batch", "serve"],
+    ap.add_argument("--workload", default="1m", choices=["1m", "batch", "serve", "pi"],
                     help="1m: the 1M x 1M product (default line); batch: 4096 uneven products; "
-                         "serve: serving loop under Poisson arrivals")
+                         "serve: serving loop under Poisson arrivals; pi: pi to 10^8 digits")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
@@ -581,6 +628,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "pi":
+        run_pi(args)
     else:
         run_ours(args)
 

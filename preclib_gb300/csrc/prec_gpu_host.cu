@@ -76,7 +76,7 @@ constexpr size_t kStatBytes = 16;       // device status block (error bits, FFT 
 constexpr size_t kFftBandMin = 192;     // src/mul_basic.cpp:4 (FFT above 192 limbs)
 constexpr size_t kFftBandMax = 6144;    // src/mul_basic.cpp:5 (NTT above 6144 limbs)
 
-static CrtConst crt_for(int set, int k) {
+static CrtConst crt_compute(int set, int k) {
     const uint32_t* P = kP[set];
     const uint32_t p1 = P[0], p2 = P[1], p3 = P[2];
     uint32_t s[kPrimes];
@@ -95,6 +95,19 @@ static CrtConst crt_for(int set, int k) {
     c.k32 = shoup(c23, p3);
     c.k33 = shoup(mulmod(s[2], c1323, p3), p3);
     return c;
+}
+
+// CRT constants of every (set, length), computed once: plan_for runs once
+// per product of a batch, and a batch can hold millions of small products
+static CrtConst crt_for(int set, int k) {
+    constexpr int K = kSetMaxLog2[kSets - 1] + 1;
+    static CrtConst table[kSets][K];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (int s = 0; s < kSets; ++s)
+            for (int j = kSmallMinLog2; j <= kSetMaxLog2[s]; ++j) table[s][j] = crt_compute(s, j);
+    });
+    return table[set][k];
 }
 
 // da, db: 32-bit digit counts (upper bounds are fine)

@@ -15,10 +15,12 @@
 //   * the square root, the final division and the decimal conversion run
 //     Newton iterations whose products go to the GPU (bignum.cpp), the
 //     conversion's splits once more as one batch per level.
-// Products of at most kHostMaxLimbs limbs (the tree's lowest levels) run
-// on the host, as the reference multiplies them with its schoolbook and
-// Karatsuba code; everything larger is computed by libprecgpu.  There is
-// no CPU path for those: without a device the program stops.
+// The tree's four lowest levels (blocks of 16 terms, products of at most
+// about 20 limbs) and any other product of at most kHostMaxLimbs limbs run
+// on the host threads, as the reference multiplies such sizes with its
+// schoolbook and Karatsuba code; everything larger is computed by
+// libprecgpu.  There is no CPU path for those: without a device the
+// program stops.  PI_GB300_TRACE=1 prints the time of every level.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -27,7 +29,6 @@
 #include <cstring>
 #include <fstream>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/prec_gpu.h"
@@ -35,12 +36,16 @@
 
 using namespace precpi;
 
+#ifndef PI_HOST_MAX_LIMBS
+#define PI_HOST_MAX_LIMBS 48
+#endif
+
 namespace {
 
 constexpr u64 kC3Over24 = 10939058860032000ull;  // 640320^3 / 24
 constexpr u64 kA = 13591409ull;
 constexpr u64 kB = 545140134ull;
-constexpr size_t kHostMaxLimbs = 32;  // products up to this size stay on the host
+constexpr size_t kHostMaxLimbs = PI_HOST_MAX_LIMBS;  // products up to this size stay on the host
 
 double now_sec() {
     static const auto t0 = std::chrono::steady_clock::now();
@@ -125,16 +130,24 @@ struct GpuBackend : MulBackend {
         });
         host_products += host.size();
         if (gpu.empty()) return;
-        // layout: each distinct operand once, then the results
-        std::unordered_map<const Nat*, size_t> where;
-        std::vector<const Nat*> uniq;
+        // layout: the operands (one copy of an operand repeated within the
+        // last few products, e.g. a shared divisor or a node used twice),
+        // then the results
+        std::vector<size_t> aoff(gpu.size()), boff(gpu.size());
+        std::vector<std::pair<const Nat*, size_t>> uniq;  // operand, offset
         size_t in = 0;
-        for (size_t i : gpu)
-            for (const Nat* x : {A[i], B[i]})
-                if (where.emplace(x, in).second) {
-                    uniq.push_back(x);
-                    in += up32(x->size());
-                }
+        auto place = [&](const Nat* x) {
+            const size_t lo = uniq.size() > 8 ? uniq.size() - 8 : 0;
+            for (size_t j = uniq.size(); j-- > lo;)
+                if (uniq[j].first == x) return uniq[j].second;
+            uniq.emplace_back(x, in);
+            in += up32(x->size());
+            return uniq.back().second;
+        };
+        for (size_t u = 0; u < gpu.size(); ++u) {
+            aoff[u] = place(A[gpu[u]]);
+            boff[u] = place(B[gpu[u]]);
+        }
         std::vector<size_t> ooff(gpu.size());
         size_t total = in;
         for (size_t u = 0; u < gpu.size(); ++u) {
@@ -143,15 +156,15 @@ struct GpuBackend : MulBackend {
         }
         reserve(total);
         parallel_for(uniq.size(), [&](size_t u) {
-            std::memcpy(h_buf + where[uniq[u]], uniq[u]->d.data(), uniq[u]->size() * sizeof(u64));
+            std::memcpy(h_buf + uniq[u].second, uniq[u].first->d.data(), uniq[u].first->size() * sizeof(u64));
         });
         check_cuda(cudaMemcpyAsync(d_buf, h_buf, in * sizeof(u64), cudaMemcpyHostToDevice, st), "H2D");
         std::vector<prec_gpu_product_t> items(gpu.size());
         for (size_t u = 0; u < gpu.size(); ++u) {
             const size_t i = gpu[u];
-            items[u].a = d_buf + where[A[i]];
+            items[u].a = d_buf + aoff[u];
             items[u].an = A[i]->size();
-            items[u].b = d_buf + where[B[i]];
+            items[u].b = d_buf + boff[u];
             items[u].bn = B[i]->size();
             items[u].out = d_buf + ooff[u];
         }
@@ -226,11 +239,44 @@ void signed_add(Nat a, bool an, Nat b, bool bn, Nat& r, bool& rn) {
     }
 }
 
+// the node of terms [a, b) by recursive halving on the host (small operands)
+Node host_split(u64 a, u64 b) {
+    if (b - a == 1) return leaf(a);
+    const u64 m = a + (b - a) / 2;
+    Node l = host_split(a, m), r = host_split(m, b);
+    auto hmul = [](const Nat& x, const Nat& y, Nat& out) {
+        out.d.assign(x.size() + y.size(), 0);
+        mul_school(x.d.data(), x.size(), y.d.data(), y.size(), out.d.data());
+        normalize(out);
+    };
+    Node u;
+    Nat t1, t2;
+    hmul(l.q, r.q, u.q);
+    hmul(l.t, r.q, t1);
+    hmul(r.t, l.p, t2);
+    hmul(l.p, r.p, u.p);
+    signed_add(std::move(t1), l.neg, std::move(t2), r.neg, u.t, u.neg);
+    return u;
+}
+
+bool trace_on() {
+    static const bool on = std::getenv("PI_GB300_TRACE") != nullptr;
+    return on;
+}
+
 // Q(0, terms) and T(0, terms)
 void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
-    std::vector<Node> lv(terms);
-    parallel_for(terms, [&](size_t k) { lv[k] = leaf(k); });
+    // the lowest levels in blocks of kHostBlock terms on the host threads:
+    // their products have at most about 20 limbs
+    constexpr size_t kHostBlock = 16;
+    double t0 = now_sec();
+    std::vector<Node> lv((terms + kHostBlock - 1) / kHostBlock);
+    parallel_for(lv.size(), [&](size_t i) {
+        lv[i] = host_split(i * kHostBlock, std::min<size_t>(terms, (i + 1) * kHostBlock));
+    });
+    if (trace_on()) std::fprintf(stderr, "  blocks of %zu terms: %zu nodes %.3f s\n", kHostBlock, lv.size(), now_sec() - t0);
     while (lv.size() > 1) {
+        t0 = now_sec();
         const size_t m = lv.size(), pairs = m / 2;
         // the last node of a level (the range ending at `terms`) never needs P
         const bool last_pair_is_last = (m % 2) == 0;
@@ -261,6 +307,9 @@ void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
         });
         if (m % 2) up.back() = std::move(lv.back());
         lv.swap(up);
+        if (trace_on())
+            std::fprintf(stderr, "  level of %zu nodes: Q of the first node %zu limbs, %.3f s\n", m, lv[0].q.size(),
+                         now_sec() - t0);
     }
     Q = std::move(lv[0].q);
     T = std::move(lv[0].t);

@@ -5,7 +5,7 @@
 //
 // Phase 1 (every block): each thread turns 8 coefficients into 4 limbs,
 // the limb carry chain is resolved per warp (ballot) and per block with a
-// block carry-in of 0, the limbs are written, and the block publishes its
+// block carry-in of 0 (one barrier), the limbs are written, and the block publishes its
 // aggregate (G = carry out, P = a carry-in would pass through).
 // Phase 2 (the last block to finish, found with a fence and an atomic
 // counter): scans the aggregates into per-block carry-ins and adds the
@@ -80,11 +80,8 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
     limbs_from_sums<kCarryLimbs>(T, prev_hi, v, gbits, G, P);
 
     uint32_t* agg = PP.scratch + 1;
-    auto cin_fn = [&](bool Gb, bool Pb) -> bool {
-        agg[bid] = (Gb ? 1u : 0u) | (Pb ? 2u : 0u);
-        return false;
-    };
-    const bool cin = block_carry(G, P, sh, cin_fn);
+    auto publish = [&](bool Gb, bool Pb) { agg[bid] = (Gb ? 1u : 0u) | (Pb ? 2u : 0u); };
+    const bool cin = block_carry_in0(G, P, sh, publish);
     limbs_finish<kCarryLimbs>(m0, PP.lout, v, gbits, cin, PP.out);
 
     // ---- phase 2: the last block resolves the carries between blocks.

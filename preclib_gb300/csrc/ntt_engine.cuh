@@ -379,6 +379,34 @@ __device__ __forceinline__ bool block_carry(bool G, bool P, BlockCarryShared& sh
     return (cl >> lane) & 1;
 }
 
+// Block-wide carry resolution with a block carry-in of 0, one barrier:
+// every warp derives its own carry-in from the warp aggregates below it;
+// thread 0 hands the block aggregate (Gb, Pb) to publish.  Returns the
+// thread's carry-in.
+template <class PublishFn>
+__device__ __forceinline__ bool block_carry_in0(bool G, bool P, BlockCarryShared& sh, PublishFn publish) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    const uint32_t gm = __ballot_sync(0xffffffffu, G);
+    const uint32_t pm = __ballot_sync(0xffffffffu, P);
+    if (lane == 0) {
+        sh.wg[warp] = (uint32_t)(carry_chain(gm, pm, false) >> 32) & 1;
+        sh.wp[warp] = pm == 0xffffffffu;
+    }
+    __syncthreads();
+    bool c = false;  // carry into this warp
+    for (int w = 0; w < warp; ++w) c = sh.wg[w] || (sh.wp[w] && c);
+    if (threadIdx.x == 0) {
+        bool Gb = false, Pb = true;
+        for (int w = 0; w < nwarps; ++w) {
+            Gb = sh.wg[w] || (sh.wp[w] && Gb);
+            Pb = Pb && sh.wp[w];
+        }
+        publish(Gb, Pb);
+    }
+    return (carry_chain(gm, pm, c) >> lane) & 1;
+}
+
 // Limbs of one thread: T_k = c_{2k} + c_{2k+1} * 2^32 folds the 32-bit
 // digit convolution onto 64-bit limbs (T < 2^123); limb value
 // v_k = lo64(T_k) + hi(T_{k-1}) with generate bit g_k.  Returns (G, P):

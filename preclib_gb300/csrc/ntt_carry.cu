@@ -138,16 +138,28 @@ void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch
     launch_crt_carry(set, args, st, batch, count, max_nblk);
 }
 
-void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev, const PrimeStreams* ps) {
+void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev, const PrimeStreams* ps,
+                      cudaEvent_t a_ready, cudaEvent_t b_ready) {
     if (ps && !ev) {
         // one chain per prime; the CRT kernel joins them
-        cudaEventRecord(ps->fork, st);
+        const bool staged = a_ready && b_ready && !args.square;
+        if (!staged) cudaEventRecord(ps->fork, st);
         for (int p = 0; p < kPrimes; ++p) {
             cudaStream_t s = ps->s[p];
-            cudaStreamWaitEvent(s, ps->fork, 0);
             ProdArgs a = args;
             a.prime0 = p;
-            launch_fwd_cols(set, a, s, nullptr, 1, 1);
+            if (staged) {
+                cudaStreamWaitEvent(s, a_ready, 0);
+                a.operand_only = 1;
+                launch_fwd_cols(set, a, s, nullptr, 1, 1);
+                cudaStreamWaitEvent(s, b_ready, 0);
+                a.operand_only = 2;
+                launch_fwd_cols(set, a, s, nullptr, 1, 1);
+                a.operand_only = 0;
+            } else {
+                cudaStreamWaitEvent(s, ps->fork, 0);
+                launch_fwd_cols(set, a, s, nullptr, 1, 1);
+            }
             launch_rows(set, a, s, nullptr, 1, 1);
             launch_inv_cols(set, a, s, nullptr, 1, 1);
             cudaEventRecord(ps->join[p], s);

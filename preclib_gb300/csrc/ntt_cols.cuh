@@ -56,9 +56,11 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
     constexpr int NP = sch_np(M, MR);
     static_assert(NP >= 2, "column transforms have at least two passes");
     const ProdPtrs P = select_product(args, batch);
-    // grid.y: prime*2 + operand, or just the prime for a square (one operand)
-    const int prime = args.prime0 + (args.square ? blockIdx.y : blockIdx.y >> 1);
-    const int operand = args.square ? 0 : blockIdx.y & 1;
+    // grid.y: prime*2 + operand, or just the prime for a square or a
+    // launch of one operand
+    const bool one = args.square || args.operand_only;
+    const int prime = args.prime0 + (one ? blockIdx.y : blockIdx.y >> 1);
+    const int operand = args.operand_only ? args.operand_only - 1 : (one ? 0 : blockIdx.y & 1);
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.tf[prime];
     const uint32_t N2 = 1u << args.k2;

@@ -43,7 +43,7 @@ struct ProdArgs {
     int prime0;         // first prime of this launch of the transform kernels (grid.y covers the rest)
     int cg;             // columns per column-pass CTA (0: default)
     int cmr;            // column pass radix cap, 4 or 6 (0: default)
-    int pad;
+    int operand_only;   // forward columns of one operand: 1 = a, 2 = b (0: both)
     CrtConst crt;
     FieldArgs f;
 };
@@ -126,8 +126,12 @@ struct PrimeStreams {
     cudaEvent_t fork;
     cudaEvent_t join[kPrimes];
 };
+// With side streams, `a_ready` / `b_ready` (recorded on `st` after each
+// operand's upload) let each prime's forward columns of a start while b is
+// still being copied.
 void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev = nullptr,
-                      const PrimeStreams* ps = nullptr);
+                      const PrimeStreams* ps = nullptr, cudaEvent_t a_ready = nullptr,
+                      cudaEvent_t b_ready = nullptr);
 // the batch form: `count` products of one length class (class-wide fields
 // from `args`, per-product fields from the device array `batch`);
 // max_nblk = the largest carry grid of the class

@@ -148,6 +148,7 @@ struct Ctx {
     double* h_maxdist = nullptr;
     double2* fft_tw = nullptr;  // FP64 band twiddles
     cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // each operand on the device
     cudaEvent_t stage_ev[kMaxStages + 1] = {};
     FieldArgs field[kSets] = {};
     PrimeStreams prime_streams = {};
@@ -247,6 +248,8 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaEventCreateWithFlags(&c.last_done, cudaEventDisableTiming));
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
+    CK(cudaEventCreateWithFlags(&c.ev_a, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c.ev_b, cudaEventDisableTiming));
     for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&c.stage_ev[i]));
     for (int p = 0; p < kPrimes; ++p) {
         CK(cudaStreamCreateWithFlags(&c.prime_streams.s[p], cudaStreamNonBlocking));
@@ -324,7 +327,8 @@ static int ensure_io(Ctx& c, size_t limbs) {
 // A square (d_a == d_b, la == lb) transforms its one operand only on the
 // four-step path; the single-CTA path reads the operand twice.
 static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
-                       uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+                       uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                       cudaEvent_t a_ready = nullptr, cudaEvent_t b_ready = nullptr) {
     const int square = (d_a == d_b && la == lb) ? 1 : 0;
     const uint64_t lout = la + lb;
     if (pl.path == 0) {
@@ -361,7 +365,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.crt = pl.crt;
         args.f = c.field[pl.set];
         const bool split = c.split_primes && pl.split;
-        ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr);
+        ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready);
     }
     CK(cudaGetLastError());
     return 0;
@@ -476,8 +480,11 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     uint64_t* d_out = c.io + la_pad + lb_pad;
     cudaStream_t st = c.stream;
     CK(cudaStreamWaitEvent(st, c.last_done, 0));
+    // the per-prime chains start on a's forward columns while b is copied
     CK(cudaMemcpyAsync(d_a, a, la * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(c.ev_a, st));
     if (!square) CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(c.ev_b, st));
     CK(cudaEventRecord(c.ev0, st));
     if (use_fft) {
         FftArgs f{};
@@ -501,7 +508,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         f.k2 = fp.k2;
         fft_launch(f, st);
         CK(cudaGetLastError());
-    } else if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st))) {
+    } else if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st, nullptr, c.ev_a, c.ev_b))) {
         return r;
     }
     CK(cudaEventRecord(c.ev1, st));
@@ -551,6 +558,8 @@ void prec_gpu_shutdown(void) {
     cudaEventDestroy(c.last_done);
     cudaEventDestroy(c.ev0);
     cudaEventDestroy(c.ev1);
+    cudaEventDestroy(c.ev_a);
+    cudaEventDestroy(c.ev_b);
     for (int i = 0; i <= kMaxStages; ++i) cudaEventDestroy(c.stage_ev[i]);
     for (int p = 0; p < kPrimes; ++p) {
         cudaStreamDestroy(c.prime_streams.s[p]);

@@ -169,3 +169,30 @@ def test_too_large_rejected(gpu):
         code = gpu.lib().prec_gpu_mul_device(1, (1 << 24) + 1, 1, 1 << 24, 1, None)
         gpu.check(code)
     assert e.value.code == gpu.E_TOO_LARGE
+
+
+def test_host_api_pinned_result_buffer(gpu):
+    """Page-locked operand and result buffers: the limbs, nothing written
+    past an + bn, and a result written over its own operand."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    L = gpu.lib()
+    for (an, bn) in ((1 << 20, 1 << 20), (40000, 30001), (2000, 100), (300, 7)):
+        a = O.splitmix64(an + 17, an)
+        b = O.splitmix64(bn + 18, bn)
+        want = O.mul_ntt(a, b)
+        ho = torch.full((an + bn + 1,), -1, dtype=torch.int64).pin_memory()
+        po = ho.numpy().view(np.uint64)
+        gpu.check(L.prec_gpu_mul_ntt(gpu._p(a), an, gpu._p(b), bn, gpu._p(po)))
+        assert np.array_equal(po[:an + bn], want), (an, bn)
+        assert po[an + bn] == np.uint64(0xFFFFFFFFFFFFFFFF)  # nothing past an + bn
+    # result written over operand a (both in page-locked memory)
+    an = bn = 50000
+    a = O.splitmix64(5, an)
+    b = O.splitmix64(6, bn)
+    want = O.mul_ntt(a, b)
+    buf = torch.zeros(an + bn, dtype=torch.int64).pin_memory()
+    pb = buf.numpy().view(np.uint64)
+    pb[:an] = a
+    gpu.check(L.prec_gpu_mul(gpu._p(pb), an, gpu._p(b), bn, gpu._p(pb)))
+    assert np.array_equal(pb, want)

@@ -87,9 +87,9 @@ int prec_gpu_sqr(const uint64_t *a, size_t an, uint64_t *out);
 
 /* ---- Autotuner ------------------------------------------------------------
  * Kernel configuration of one four-step NTT length 2^log2_n (13 .. 26):
- * the column/row split, columns per column-pass CTA, the column pass radix
- * cap, rows per row-pass CTA, and whether a single product runs each
- * prime's kernels on its own stream.  Every product (single, batch,
+ * the column/row split, columns per column-pass CTA, the column and row
+ * pass radix caps, rows per row-pass CTA, and whether a single product
+ * runs each prime's kernels on its own stream.  Every product (single, batch,
  * serving loop) uses the configuration of its length.  Defaults apply until
  * a length is tuned, set or loaded; PREC_GPU_TUNE_FILE names a table that
  * prec_gpu_init loads. */
@@ -98,6 +98,7 @@ typedef struct {
     int log2_cols;      /* column length 2^log2_cols, row length 2^(log2_n - log2_cols) */
     int col_group;      /* columns per column-pass CTA: 4 or 8 */
     int col_radix_cap;  /* largest radix 2^cap of a column pass: 4 or 6 */
+    int row_radix_cap;  /* largest radix 2^cap of a row pass: 4 or 6 */
     int rows_per_cta;   /* rows per row-pass CTA */
     int split_primes;   /* 1: per-prime stream chains for a single product */
     float ms;           /* measured product time (0: not measured) */
@@ -107,7 +108,7 @@ typedef struct {
 /* Times the configurations of every length 2^kmin .. 2^kmax (clamped to
  * 13 .. 26) on the current device with balanced random operands of
  * 2^(k-2) limbs each, by coordinate descent from the default (per-prime
- * streams, rows per CTA, columns per CTA, radix cap, then the column/row
+ * streams, rows per CTA, columns per CTA, radix caps, then the column/row
  * split).  A candidate counts only if its product equals the default
  * configuration's bit for bit; the fastest is installed.  Writes up to
  * `cap` entries to `out` (may be NULL) and the number of lengths to *count. */

@@ -174,10 +174,10 @@ __device__ __forceinline__ void regs_pass(uint32_t (&x)[NA][Geom<M, T, MR>::R], 
 
 // Row layout: array a at sm + a*astride, element i at P(i).  Items of NA
 // arrays share twiddle loads.  narr must be a multiple of NA.
-template <int SET, int M, int T, bool DIT, int NA>
+template <int SET, int M, int T, bool DIT, int NA, int MR = PREC_SCH_MAXRB>
 __device__ __forceinline__ void row_pass(uint32_t* sm, int astride, int narr, const uint2* __restrict__ tw,
                                          const PrimeC& c) {
-    using G = Geom<M, T>;
+    using G = Geom<M, T, MR>;
     const int total = (narr / NA) << G::LGI;
 #pragma unroll kPassUnroll
     for (int w = threadIdx.x; w < total; w += blockDim.x) {
@@ -189,7 +189,7 @@ __device__ __forceinline__ void row_pass(uint32_t* sm, int astride, int narr, co
         for (int a = 0; a < NA; ++a)
 #pragma unroll
             for (int q = 0; q < G::R; ++q) x[a][q] = s[a * astride + q * G::QS];
-        regs_pass<SET, M, T, DIT, NA>(x, u, tw, c);
+        regs_pass<SET, M, T, DIT, NA, MR>(x, u, tw, c);
 #pragma unroll
         for (int a = 0; a < NA; ++a)
 #pragma unroll
@@ -275,13 +275,13 @@ __device__ __forceinline__ void col_pass(uint32_t* sm, const uint2* __restrict__
 }
 
 // Middle passes T in [T0, T1] (ascending for DIF, descending for DIT).
-template <int SET, int M, int T, int TEND, bool DIT, int NA>
+template <int SET, int M, int T, int TEND, bool DIT, int NA, int MR = PREC_SCH_MAXRB>
 __device__ __forceinline__ void row_passes(uint32_t* sm, int astride, int narr, const uint2* __restrict__ tw,
                                            const PrimeC& c) {
     if constexpr (DIT ? (T >= TEND) : (T <= TEND)) {
-        row_pass<SET, M, T, DIT, NA>(sm, astride, narr, tw, c);
+        row_pass<SET, M, T, DIT, NA, MR>(sm, astride, narr, tw, c);
         __syncthreads();
-        row_passes<SET, M, DIT ? T - 1 : T + 1, TEND, DIT, NA>(sm, astride, narr, tw, c);
+        row_passes<SET, M, DIT ? T - 1 : T + 1, TEND, DIT, NA, MR>(sm, astride, narr, tw, c);
     }
 }
 

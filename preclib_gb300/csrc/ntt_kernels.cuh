@@ -44,6 +44,8 @@ struct ProdArgs {
     int cg;             // columns per column-pass CTA (0: default)
     int cmr;            // column pass radix cap, 4 or 6 (0: default)
     int operand_only;   // forward columns of one operand: 1 = a, 2 = b (0: both)
+    int rmr;            // row pass radix cap, 4 or 6 (0: default)
+    int pad;
     CrtConst crt;
     FieldArgs f;
 };
@@ -157,6 +159,15 @@ int configure_inv_cols();
 // the requested columns per CTA and radix cap (0 = default: 8 columns,
 // radix cap 6).  The radix cap only changes the schedule of 2^10- and
 // 2^11-point columns; set 1's 2^12- and 2^13-point columns take 4 columns.
+// Row-pass radix cap instantiated for m = log2 N2 (0 = default): the cap
+// changes the schedule of 2^10- and 2^11-point rows only; by default 2^10
+// rows run as two radix-32 passes (7% faster on GB300) and 2^11 rows as
+// radix-8, -8, -32 passes (a radix-64 pass costs them registers).
+inline int row_radix_cap(int m, int req) {
+    if (m != 10 && m != 11) return 4;
+    return req == 4 || req == 6 ? req : (m == 10 ? 6 : 4);
+}
+
 inline void col_config(int set, int m, int req_cg, int req_mr, int& cg, int& mr) {
     cg = (req_cg == 4 || req_cg == 8) ? req_cg : kColGroup;
     if (set == 1 && m >= 12) cg = 4;

@@ -31,10 +31,13 @@ namespace precgpu {
 
 constexpr int kRowsTopUnroll = PREC_ROWS_TOP_UNROLL;  // items of the top pass in flight per thread
 
-template <int SET, int M, bool SQ>
-__global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, const ProdPtrs* __restrict__ batch) {
+// MR: pass radix cap.  With MR = 6 a 2^11-point row runs as a radix-64 and
+// a radix-32 pass (no middle pass); the radix-64 top pass then takes the two
+// operands one after the other (64 values in registers, not 128).
+template <int SET, int M, bool SQ, int MR>
+__global__ void __launch_bounds__(256, MR == 6 ? 2 : PREC_ROWS_MINB) k_rows(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
-    constexpr int NP = sch_np(M);
+    constexpr int NP = sch_np(M, MR);
     static_assert(NP >= 2, "row transforms have at least two passes");
     constexpr int AS = astride_for(M);
     const ProdPtrs P = select_product(args, batch);
@@ -49,32 +52,38 @@ __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, con
     constexpr int NA = SQ ? 1 : 2;  // a square transforms its one operand only
 
     {   // top DIF pass of A (and B) straight from HBM (shared twiddles)
-        using G = Geom<M, 0>;
+        using G = Geom<M, 0, MR>;
+        constexpr bool SEQ = !SQ && G::R > 32;  // operands one after the other
+        constexpr int NT = SEQ ? 1 : NA;        // operands per item
+        constexpr int items = 1 << G::LGI;
 #pragma unroll kRowsTopUnroll
-        for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
-            const int r = w >> G::LGI;
-            const uint32_t u = w & ((1u << G::LGI) - 1);
+        for (int w = threadIdx.x; w < (rows * items) * (SEQ ? 2 : 1); w += blockDim.x) {
+            const int op = SEQ ? w / (rows * items) : 0;
+            const int wi = SEQ ? w - op * (rows * items) : w;
+            const int r = wi >> G::LGI;
+            const uint32_t u = wi & (items - 1);
             const uint64_t roff = ((uint64_t)(row0 + r) << M) + G::base(u);
-            uint32_t x[NA][G::R];
+            const uint32_t* __restrict__ src = op ? B : A;
+            uint32_t x[NT][G::R];
 #pragma unroll
             for (int q = 0; q < G::R; ++q) {
-                x[0][q] = A[roff + ((uint32_t)q << G::LO)];
-                if constexpr (!SQ) x[NA - 1][q] = B[roff + ((uint32_t)q << G::LO)];
+                x[0][q] = src[roff + ((uint32_t)q << G::LO)];
+                if constexpr (NT == 2) x[1][q] = B[roff + ((uint32_t)q << G::LO)];
             }
-            regs_pass<SET, M, 0, false, NA>(x, u, twf, pc);
-            uint32_t* s = sm + 2 * r * AS + G::pbase(u);
+            regs_pass<SET, M, 0, false, NT, MR>(x, u, twf, pc);
+            uint32_t* s = sm + 2 * r * AS + op * AS + G::pbase(u);
 #pragma unroll
             for (int q = 0; q < G::R; ++q) {
                 s[q * G::QS] = x[0][q];
-                if constexpr (!SQ) s[AS + q * G::QS] = x[NA - 1][q];
+                if constexpr (NT == 2) s[AS + q * G::QS] = x[1][q];
             }
         }
         __syncthreads();
     }
-    if constexpr (SQ) row_passes<SET, M, 1, NP - 2, false, 1>(sm, 2 * AS, rows, twf, pc);
-    else row_passes<SET, M, 1, NP - 2, false, 2>(sm, AS, 2 * rows, twf, pc);
+    if constexpr (SQ) row_passes<SET, M, 1, NP - 2, false, 1, MR>(sm, 2 * AS, rows, twf, pc);
+    else row_passes<SET, M, 1, NP - 2, false, 2, MR>(sm, AS, 2 * rows, twf, pc);
     {   // bottom: last DIF stages, product, first DIT stages
-        using G = Geom<M, NP - 1>;
+        using G = Geom<M, NP - 1, MR>;
         static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
         for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
             const int r = w >> G::LGI;
@@ -86,19 +95,19 @@ __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, con
                 x[0][q] = s[q];
                 if constexpr (!SQ) x[NA - 1][q] = s[AS + q];
             }
-            regs_pass<SET, M, NP - 1, false, NA>(x, u, twf, pc);
+            regs_pass<SET, M, NP - 1, false, NA, MR>(x, u, twf, pc);
             uint32_t y[1][32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) y[0][q] = Ar<SET>::mul(x[0][q], x[NA - 1][q], pc);
-            regs_pass<SET, M, NP - 1, true, 1>(y, u, twi, pc);
+            regs_pass<SET, M, NP - 1, true, 1, MR>(y, u, twi, pc);
 #pragma unroll
             for (int q = 0; q < 32; ++q) s[q] = y[0][q];
         }
         __syncthreads();
     }
-    row_passes<SET, M, NP - 2, 1, true, 1>(sm, 2 * AS, rows, twi, pc);
+    row_passes<SET, M, NP - 2, 1, true, 1, MR>(sm, 2 * AS, rows, twi, pc);
     {   // top DIT pass with the inverse four-step twiddle, straight to HBM
-        using G = Geom<M, 0>;
+        using G = Geom<M, 0, MR>;
         const uint32_t nmask = (uint32_t)((1ull << args.k) - 1);
         for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
             const int r = w >> G::LGI;
@@ -107,7 +116,7 @@ __global__ void __launch_bounds__(256, PREC_ROWS_MINB) k_rows(ProdArgs args, con
             uint32_t x[1][G::R];
 #pragma unroll
             for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS];
-            regs_pass<SET, M, 0, true, 1>(x, u, twi, pc);
+            regs_pass<SET, M, 0, true, 1, MR>(x, u, twi, pc);
             // element q is i2 = base + (q << LO); twiddle w^-(i2*k1) = t * g^q
             const uint32_t srow = row0 + r;
             const uint32_t k1v = brev_bits(srow, args.k1);
@@ -141,7 +150,10 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
     return rows << (k2 - 5);
 }
 
-#define PREC_ROWS1(X, SQ) X(0, 7, SQ) X(0, 8, SQ) X(0, 9, SQ) X(0, 10, SQ) X(0, 11, SQ) X(0, 12, SQ) X(1, 13, SQ)
+// (set, M, radix cap): the cap changes the schedule of 2^10- and 2^11-point rows only
+#define PREC_ROWS1(X, SQ)                                                                                      \
+    X(0, 7, SQ, 4) X(0, 8, SQ, 4) X(0, 9, SQ, 4) X(0, 10, SQ, 4) X(0, 10, SQ, 6) X(0, 11, SQ, 4) X(0, 11, SQ, 6) \
+    X(0, 12, SQ, 4) X(1, 13, SQ, 4)
 #define PREC_ROWS(X) PREC_ROWS1(X, false) PREC_ROWS1(X, true)
 
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
@@ -149,16 +161,20 @@ void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* ba
     const dim3 grid((1u << a.k1) / a.rows, nprimes, count);
     const int threads = a.rows << (m - 5);
     const size_t smem = row_smem(m, a.rows);
-#define X(S, MM, SQ) \
-    if (set == S && m == MM && (a.square != 0) == SQ) { k_rows<S, MM, SQ><<<grid, threads, smem, st>>>(a, batch); return; }
+    const int mr = row_radix_cap(m, a.rmr);
+#define X(S, MM, SQ, RR)                                                                  \
+    if (set == S && m == MM && (a.square != 0) == SQ && mr == RR) {                       \
+        k_rows<S, MM, SQ, RR><<<grid, threads, smem, st>>>(a, batch);                     \
+        return;                                                                         \
+    }
     PREC_ROWS(X)
 #undef X
 }
 
 int configure_rows() {
     cudaError_t e = cudaSuccess;
-#define X(S, MM, SQ)                                                                                   \
-    if (!e) e = cudaFuncSetAttribute(k_rows<S, MM, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+#define X(S, MM, SQ, RR)                                                                                      \
+    if (!e) e = cudaFuncSetAttribute(k_rows<S, MM, SQ, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
                                      (int)row_smem(MM, 256 >> (MM - 5) > 0 ? 256 >> (MM - 5) : 1));
     PREC_ROWS(X)
 #undef X

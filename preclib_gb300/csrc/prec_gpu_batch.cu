@@ -119,6 +119,7 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
             args.rows = c.pl.rows;
             args.cg = c.pl.cg;
             args.cmr = c.pl.cmr;
+            args.rmr = c.pl.rmr;
             args.square = c.square;
             args.crt = c.pl.crt;
             args.f = ctx_field(c.pl.set);

@@ -361,6 +361,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.rows = pl.rows;
         args.cg = pl.cg;
         args.cmr = pl.cmr;
+        args.rmr = pl.rmr;
         args.square = square;
         args.crt = pl.crt;
         args.f = c.field[pl.set];

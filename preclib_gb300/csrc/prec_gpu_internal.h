@@ -21,6 +21,7 @@ struct Plan {
     int rows = 0;  // rows per CTA of the row pass
     int cg = 0;    // columns per column-pass CTA (0: default)
     int cmr = 0;   // column pass radix cap (0: default)
+    int rmr = 0;   // row pass radix cap (0: default)
     int split = 0; // per-prime stream chains for a single product
     CrtConst crt{};
     size_t work_bytes = 0;  // work buffer + carry words of the four-step path
@@ -37,6 +38,7 @@ struct KernelConfig {
     int k1 = 0;     // log2 column length (row length 2^(k - k1))
     int cg = 0;     // columns per column-pass CTA: 4 or 8
     int cmr = 0;    // column pass radix cap: 4 or 6
+    int rmr = 0;    // row pass radix cap: 4 or 6
     int rows = 0;   // rows per row-pass CTA
     int split = 0;  // per-prime stream chains
 };

@@ -119,6 +119,7 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         args.rows = r.pl.rows;
         args.cg = r.pl.cg;
         args.cmr = r.pl.cmr;
+        args.rmr = r.pl.rmr;
         args.crt = r.pl.crt;
         args.f = ctx_field(r.pl.set);
         ntt_launch_4step(r.pl.set, args, st);

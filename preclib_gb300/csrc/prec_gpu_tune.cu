@@ -56,6 +56,7 @@ KernelConfig default_config(int k) {
     col_config(set, c.k1, 0, 0, cg, mr);
     c.cg = cg;
     c.cmr = mr;
+    c.rmr = row_radix_cap(k - c.k1, 0);
     ntt_row_threads(k - c.k1, 1 << c.k1, &c.rows);
     c.split = k >= kSplitMinLog2 ? 1 : 0;
     return c;
@@ -72,6 +73,7 @@ bool config_valid(int k, const KernelConfig& c) {
     if (c.cg != 4 && c.cg != 8) return false;
     if (set == 1 && c.k1 >= 12 && c.cg != 4) return false;
     if (c.cmr != 4 && c.cmr != 6) return false;
+    if (c.rmr != 4 && c.rmr != 6) return false;
     if (!pow2(c.rows) || c.rows > (1 << c.k1)) return false;
     const int threads = c.rows << (k2 - 5);
     if (threads < 32 || threads > 256) return false;
@@ -91,6 +93,7 @@ void apply_config(Plan& pl, const KernelConfig& c) {
     pl.k2 = pl.k - c.k1;
     pl.cg = c.cg;
     pl.cmr = c.cmr;
+    pl.rmr = c.rmr;
     pl.rows = c.rows;
     pl.split = c.split;
 }
@@ -116,6 +119,7 @@ void to_entry(int k, const KernelConfig& c, float ms, float dms, prec_gpu_tune_e
     e->log2_cols = c.k1;
     e->col_group = c.cg;
     e->col_radix_cap = c.cmr;
+    e->row_radix_cap = c.rmr;
     e->rows_per_cta = c.rows;
     e->split_primes = c.split;
     e->ms = ms;
@@ -127,13 +131,15 @@ KernelConfig from_entry(const prec_gpu_tune_entry_t* e) {
     c.k1 = e->log2_cols;
     c.cg = e->col_group;
     c.cmr = e->col_radix_cap;
+    c.rmr = e->row_radix_cap;
     c.rows = e->rows_per_cta;
     c.split = e->split_primes;
     return c;
 }
 
 bool same(const KernelConfig& a, const KernelConfig& b) {
-    return a.k1 == b.k1 && a.cg == b.cg && a.cmr == b.cmr && a.rows == b.rows && a.split == b.split;
+    return a.k1 == b.k1 && a.cg == b.cg && a.cmr == b.cmr && a.rmr == b.rmr && a.rows == b.rows &&
+           a.split == b.split;
 }
 
 // Device buffers and timing of one tuning run.
@@ -250,6 +256,11 @@ int tune_one(Tuner& T, int k, KernelConfig& best, float& best_ms, float& default
         c.cmr = c.cmr == 6 ? 4 : 6;
         consider(c);
     }
+    {
+        KernelConfig c = best;
+        c.rmr = c.rmr == 6 ? 4 : 6;
+        consider(c);
+    }
     const KernelConfig before = best;
     for (int d = -1; d <= 1; d += 2) {
         KernelConfig c = before;
@@ -259,6 +270,7 @@ int tune_one(Tuner& T, int k, KernelConfig& best, float& best_ms, float& default
         col_config(set_of(k), c.k1, c.cg, c.cmr, cg, mr);
         c.cg = cg;
         c.cmr = mr;
+        c.rmr = row_radix_cap(k - c.k1, 0);
         ntt_row_threads(k - c.k1, 1 << c.k1, &c.rows);
         consider(c);
     }
@@ -333,19 +345,20 @@ int prec_gpu_tune_reset(void) {
     return PREC_GPU_OK;
 }
 
-// Text format: a header line "# prec_gpu tune 1", then per tuned length
-// "log2_n log2_cols col_group col_radix_cap rows_per_cta split_primes ms default_ms".
+// Text format: a header line "# prec_gpu tune 2", then per tuned length
+// "log2_n log2_cols col_group col_radix_cap row_radix_cap rows_per_cta
+// split_primes ms default_ms".
 int prec_gpu_tune_save(const char* path) {
     if (!path) return PREC_GPU_E_ARG;
     FILE* f = std::fopen(path, "w");
     if (!f) return PREC_GPU_E_ARG;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    std::fprintf(f, "# prec_gpu tune 1\n");
+    std::fprintf(f, "# prec_gpu tune 2\n");
     for (int k = kTuneMin; k <= kTuneMax; ++k) {
         const Entry& t = g_tune[k];
         if (!t.tuned) continue;
-        std::fprintf(f, "%d %d %d %d %d %d %.6f %.6f\n", k, t.cfg.k1, t.cfg.cg, t.cfg.cmr, t.cfg.rows, t.cfg.split,
-                     t.ms, t.default_ms);
+        std::fprintf(f, "%d %d %d %d %d %d %d %.6f %.6f\n", k, t.cfg.k1, t.cfg.cg, t.cfg.cmr, t.cfg.rmr, t.cfg.rows,
+                     t.cfg.split, t.ms, t.default_ms);
     }
     const bool ok = std::fclose(f) == 0;
     return ok ? PREC_GPU_OK : PREC_GPU_E_ARG;
@@ -360,7 +373,7 @@ int prec_gpu_tune_load(const char* path) {
     bool header = false, bad = false;
     while (std::fgets(line, sizeof line, f)) {
         if (!header) {
-            header = std::strncmp(line, "# prec_gpu tune 1", 17) == 0;
+            header = std::strncmp(line, "# prec_gpu tune 2", 17) == 0;
             if (!header) {
                 bad = true;
                 break;
@@ -369,8 +382,8 @@ int prec_gpu_tune_load(const char* path) {
         }
         if (line[0] == '\n' || line[0] == '#') continue;
         prec_gpu_tune_entry_t e{};
-        if (std::sscanf(line, "%d %d %d %d %d %d %f %f", &e.log2_n, &e.log2_cols, &e.col_group, &e.col_radix_cap,
-                        &e.rows_per_cta, &e.split_primes, &e.ms, &e.default_ms) != 8 ||
+        if (std::sscanf(line, "%d %d %d %d %d %d %d %f %f", &e.log2_n, &e.log2_cols, &e.col_group, &e.col_radix_cap,
+                        &e.row_radix_cap, &e.rows_per_cta, &e.split_primes, &e.ms, &e.default_ms) != 9 ||
             !config_valid(e.log2_n, from_entry(&e))) {
             bad = true;
             break;

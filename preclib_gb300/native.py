@@ -48,7 +48,8 @@ class Product(ctypes.Structure):
 class TuneEntry(ctypes.Structure):
     """prec_gpu_tune_entry_t: kernel configuration of one NTT length."""
     _fields_ = [("log2_n", ctypes.c_int), ("log2_cols", ctypes.c_int), ("col_group", ctypes.c_int),
-                ("col_radix_cap", ctypes.c_int), ("rows_per_cta", ctypes.c_int), ("split_primes", ctypes.c_int),
+                ("col_radix_cap", ctypes.c_int), ("row_radix_cap", ctypes.c_int), ("rows_per_cta", ctypes.c_int),
+                ("split_primes", ctypes.c_int),
                 ("ms", ctypes.c_float), ("default_ms", ctypes.c_float)]
 
     def as_dict(self):

@@ -20,8 +20,10 @@ def _reset(gpu):
 
 def _configs(gpu, k):
     out = []
-    for k1, cg, cmr, rows, split in itertools.product(range(5, 14), (4, 8), (4, 6), (1, 2, 4, 8, 16, 32), (0, 1)):
-        cfg = dict(log2_n=k, log2_cols=k1, col_group=cg, col_radix_cap=cmr, rows_per_cta=rows, split_primes=split)
+    for k1, cg, cmr, rmr, rows, split in itertools.product(range(5, 14), (4, 8), (4, 6), (4, 6), (1, 2, 4, 8, 16, 32),
+                                                           (0, 1)):
+        cfg = dict(log2_n=k, log2_cols=k1, col_group=cg, col_radix_cap=cmr, row_radix_cap=rmr, rows_per_cta=rows,
+                   split_primes=split)
         try:
             gpu.tune_set(**cfg)
         except gpu.PrecGpuError:

@@ -244,6 +244,7 @@ def run_ours(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
+    launches0 = native.launch_count()
     with Clocks(local) as clk:
         for i in range(args.steps):
             evs[i][0].record(stream)
@@ -251,6 +252,7 @@ def run_ours(args):
             evs[i][1].record(stream)
             flush.fill_(i & 0xFF)
         torch.cuda.synchronize(dev)
+    launches = native.launch_count() - launches0
     clocks = clk.summary()
     native.stream_check(sptr)
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
@@ -338,7 +340,7 @@ def run_ours(args):
                                  "unit": "GB/s"},
             "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": 8 * (AN + BN),
                     "d2h_bytes_per_step": 8 * (AN + BN)},
-            "gpu_launches": (3 * 3 + 1) * args.steps,
+            "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
@@ -395,10 +397,12 @@ def run_batch(args):
     for _ in range(args.warmup):
         batched_e2e()
     native.stream_check(sptr)
+    launches0 = native.launch_count()
     t = time.perf_counter()
     for _ in range(args.steps):
         batched_e2e()
     batched_s = (time.perf_counter() - t) / args.steps
+    launches = native.launch_count() - launches0
     batched_out = host_out.numpy().view(np.uint64).copy()
     # device-resident batch (graph replay only)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -457,7 +461,7 @@ def run_batch(args):
                      "fields": "log2_cols, col_group, col_radix_cap, rows_per_cta, split_primes"},
         "e2e": {"value": round(n / batched_s, 1), "unit": "products/s", "h2d_bytes_per_step": 8 * o,
                 "d2h_bytes_per_step": 8 * o},
-        "gpu_launches": None,
+        "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)
 
@@ -532,6 +536,7 @@ def run_serve(args):
         mismatches += h1 != h2
     del out
     loads = []
+    launches0 = native.launch_count()
     for load in (0.1, 0.3, 0.5, 0.7, 0.9):
         reqs, tot = make(n_load)
         out = torch.empty(tot, dtype=torch.int64, device=dev)
@@ -554,6 +559,7 @@ def run_serve(args):
         "loads": loads,
         "peak_in_flight": st.peak_in_flight, "peak_workspace_bytes": st.peak_bytes,
         "mismatches_alone_vs_mixed": int(mismatches), "checked": len(range(0, n_cap, 20)),
+        "gpu_launches": native.launch_count() - launches0,
     }
     print(json.dumps(line), flush=True)
 
@@ -572,7 +578,7 @@ def run_pi(args):
     with open(os.path.join(ROOT, "tests", "golden", "pi.json")) as f:
         want = {r["digits"]: r for r in json.load(f)["runs"]}[PI_DIGITS]
     steps = max(1, min(args.steps, 3))
-    runs, exact = [], True
+    runs, exact, launches = [], True, None
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "pi.txt")
         for i in range(1 + steps):  # one untimed warm-up run
@@ -588,6 +594,8 @@ def run_pi(args):
                 parts = line.split()
                 if len(parts) == 3 and parts[2] == "sec":
                     ph[parts[0]] = float(parts[1])
+                if len(parts) == 2 and parts[0] == "gpu_launches":
+                    launches = int(parts[1])
             if i:
                 runs.append((wall, ph))
     wall = statistics.median(w for w, _ in runs)
@@ -600,7 +608,7 @@ def run_pi(args):
                    "l2": "n/a (whole program)"},
         "phases_s": phases, "bit_exact": bool(exact),
         "e2e": {"value": round(wall, 3), "unit": "s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
-        "gpu_launches": None,
+        "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)
 

@@ -128,6 +128,11 @@ int prec_gpu_tune_reset(void);
 int prec_gpu_tune_save(const char *path);
 int prec_gpu_tune_load(const char *path);
 
+/* Kernel launches the library has issued in this process (every product,
+ * batch graph replays included): a caller's own count of the GPU work
+ * behind its calls. */
+uint64_t prec_gpu_launch_count(void);
+
 /* Digit width (bits) the FP64 band uses for an x bn limbs; 0 outside the band. */
 int prec_gpu_fft_digit_bits(size_t an, size_t bn);
 

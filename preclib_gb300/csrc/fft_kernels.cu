@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "fft_kernels.cuh"
+#include "ntt_kernels.cuh"
 
 namespace precgpu {
 
@@ -313,6 +314,7 @@ size_t fft_table_bytes() { return (size_t)sizeof(double2) << (kFftMaxLog2 - 1); 
 
 void fft_build_table(double2* tw, cudaStream_t st) {
     k_fft_table<<<(1 << (kFftMaxLog2 - 1)) / 256, 256, 0, st>>>(tw);
+    count_launches(1);
 }
 
 static size_t cols_smem(int k1) { return (size_t)kFftCols * (fpad_host(1 << k1) + 1) * sizeof(double2); }
@@ -339,6 +341,7 @@ void fft_launch(const FftArgs& f, cudaStream_t st, cudaEvent_t* ev) {
     k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
     if (ev) cudaEventRecord(ev[3], st);
     k_fft_carry<<<1, 1024, 0, st>>>(f);
+    count_launches(4);
     if (ev) cudaEventRecord(ev[4], st);
 }
 

@@ -128,6 +128,7 @@ void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtr
     const dim3 grid(batch ? max_nblk : a.nblk, 1, count);
     if (set == 0) k_crt_carry<0><<<grid, kCarryThreads, 0, st>>>(a, batch);
     else k_crt_carry<1><<<grid, kCarryThreads, 0, st>>>(a, batch);
+    count_launches(1);
 }
 
 void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch, int count, int max_nblk,

@@ -12,6 +12,7 @@ void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
 #define X(S, MM, CC, RR)                                                     \
     if (set == S && a.k1 == MM && cg == CC && mr == RR) {                     \
         k_fwd_cols<S, MM, CC, RR><<<grid, 256, smem, st>>>(a, batch);         \
+        count_launches(1);                                                  \
         return;                                                             \
     }
     PREC_COLS_CONFIGS(X)

@@ -93,7 +93,7 @@ struct SmallDesc {
     uint64_t* out;
     uint64_t la, lb, lout;
     int k;
-    int square;  // a == b: one operand transform, pointwise square
+    int square;  // a == b (the single-CTA kernel reads the operand twice)
     CrtConst crt;
 };
 
@@ -113,6 +113,13 @@ constexpr int kCarryThreads = 256;
 #endif
 constexpr int kCarryLimbs = PREC_CARRY_LIMBS;  // limbs per thread in the carry kernel
 constexpr int kColGroup = PREC_COL_GROUP;      // adjacent columns per column-pass CTA (4 when N1 = 2^13)
+
+// Kernel launches issued by the library (process-wide, prec_gpu_launch_count);
+// every launcher adds its launches.  launches_this_thread() lets a graph
+// capture take back the launches it only recorded.
+void count_launches(uint64_t n);
+uint64_t launches_this_thread();
+void uncount_launches(uint64_t n);
 
 // host-side launchers; `ev` (optional) gets an event recorded before the
 // first kernel and after each kernel.

@@ -165,6 +165,7 @@ void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* ba
 #define X(S, MM, SQ, RR)                                                                  \
     if (set == S && m == MM && (a.square != 0) == SQ && mr == RR) {                       \
         k_rows<S, MM, SQ, RR><<<grid, threads, smem, st>>>(a, batch);                     \
+        count_launches(1);                                                              \
         return;                                                                         \
     }
     PREC_ROWS(X)

@@ -71,6 +71,7 @@ struct prec_gpu_batch {
     cudaEvent_t fork = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    uint64_t graph_launches = 0;  // kernels in the captured graph
     int* err = nullptr;
 };
 
@@ -256,13 +257,19 @@ int prec_gpu_batch_run(prec_gpu_batch_t* b, void* stream) {
     if (!b->exec) {
         cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_code(e);
+        const uint64_t before = launches_this_thread();
         batch_enqueue(b, b->cap, true);
+        // captured, not launched: counted at every replay instead
+        b->graph_launches = launches_this_thread() - before;
+        uncount_launches(b->graph_launches);
         e = cudaStreamEndCapture(b->cap, &b->graph);
         if (e != cudaSuccess) return cuda_code(e);
         e = cudaGraphInstantiate(&b->exec, b->graph, 0);
         if (e != cudaSuccess) return cuda_code(e);
     }
-    return cuda_code(cudaGraphLaunch(b->exec, st));
+    const cudaError_t e = cudaGraphLaunch(b->exec, st);
+    if (e == cudaSuccess) count_launches(b->graph_launches);
+    return cuda_code(e);
 }
 
 int prec_gpu_batch_info(const prec_gpu_batch_t* b, size_t* classes, size_t* device_bytes) {

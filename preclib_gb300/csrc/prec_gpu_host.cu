@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -156,6 +157,19 @@ struct Ctx {
 };
 
 static Ctx g_ctx;
+
+static std::atomic<uint64_t> g_launches{0};
+static thread_local uint64_t t_launches = 0;
+
+void count_launches(uint64_t n) {
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+    t_launches += n;
+}
+uint64_t launches_this_thread() { return t_launches; }
+void uncount_launches(uint64_t n) {
+    g_launches.fetch_sub(n, std::memory_order_relaxed);
+    t_launches -= n;
+}
 static thread_local prec_gpu_stats_t t_stats;
 
 int cuda_code(cudaError_t e) {
@@ -659,6 +673,8 @@ int prec_gpu_last_stats(prec_gpu_stats_t* st) {
     *st = t_stats;
     return 0;
 }
+
+uint64_t prec_gpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int prec_gpu_ntt_log2(size_t an, size_t bn) {
     if (an == 0 || bn == 0) return 0;

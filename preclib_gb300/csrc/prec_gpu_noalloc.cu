@@ -154,6 +154,7 @@ static int noalloc_setup(int dev, cudaStream_t stream, NoAllocDevice*& out) {
         if (e != cudaSuccess) return na_code(e);
         k_noalloc_tables<<<dim3(kTabEntries / 256, kPrimes), 256, 0, stream>>>(
             static_cast<uint8_t*>(tables), kNaP[0], kNaP[1], kNaP[2], kNaG[0], kNaG[1], kNaG[2]);
+        count_launches(1);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) return na_code(e);

@@ -27,7 +27,7 @@ EXPORTS = (
     "prec_gpu_batch_destroy", "prec_gpu_mul_batch", "prec_gpu_serve_create", "prec_gpu_serve_submit",
     "prec_gpu_serve_wait", "prec_gpu_serve_drain", "prec_gpu_serve_stats", "prec_gpu_serve_destroy",
     "prec_gpu_sqr", "prec_gpu_autotune", "prec_gpu_tune_get", "prec_gpu_tune_set", "prec_gpu_tune_reset",
-    "prec_gpu_tune_save", "prec_gpu_tune_load",
+    "prec_gpu_tune_save", "prec_gpu_tune_load", "prec_gpu_launch_count",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -89,6 +89,8 @@ def lib() -> ctypes.CDLL:
             f.restype = ctypes.c_int
         L.prec_gpu_sqr.argtypes = [_u64p, ctypes.c_size_t, _u64p]
         L.prec_gpu_sqr.restype = ctypes.c_int
+        L.prec_gpu_launch_count.argtypes = []
+        L.prec_gpu_launch_count.restype = ctypes.c_uint64
         L.prec_gpu_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneEntry), ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t)]
         L.prec_gpu_autotune.restype = ctypes.c_int
@@ -205,6 +207,11 @@ def autotune(kmin: int = 13, kmax: int = 26):
     n = ctypes.c_size_t(0)
     check(lib().prec_gpu_autotune(kmin, kmax, arr, cap, ctypes.byref(n)), "prec_gpu_autotune")
     return [arr[i].as_dict() for i in range(min(n.value, cap))]
+
+
+def launch_count() -> int:
+    """Kernel launches the library has issued in this process."""
+    return int(lib().prec_gpu_launch_count())
 
 
 def tune_get(log2_n: int) -> dict:

@@ -395,6 +395,7 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu\n", be.gpu_products,
                      be.host_products, be.batches);
     }
+    std::fprintf(stderr, "gpu_launches %llu\n", (unsigned long long)prec_gpu_launch_count());
     if (!file.empty()) std::fprintf(stderr, "wrote %s\n", file.c_str());
     std::fprintf(stderr, "time %.6f sec\n", sec);
     return 0;

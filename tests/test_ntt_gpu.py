@@ -196,3 +196,30 @@ def test_host_api_pinned_result_buffer(gpu):
     pb[:an] = a
     gpu.check(L.prec_gpu_mul(gpu._p(pb), an, gpu._p(b), bn, gpu._p(pb)))
     assert np.array_equal(pb, want)
+
+
+def test_launch_count(gpu):
+    """prec_gpu_launch_count: 10 kernels for a 2^22-point product (three per
+    prime on side streams, then the CRT), 1 for a single-CTA product, and a
+    batch graph's kernels at every replay."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 20
+    ta = torch.from_numpy(O.splitmix64(1, n).view(np.int64)).cuda()
+    to = torch.empty(2 * n, dtype=torch.int64, device="cuda")
+    c0 = gpu.launch_count()
+    gpu.mul_device(ta.data_ptr(), n, ta.data_ptr() + 8 * 7, n - 7, to.data_ptr())
+    gpu.stream_check()
+    assert gpu.launch_count() - c0 == 10
+    c0 = gpu.launch_count()
+    gpu.mul_device(ta.data_ptr(), 100, ta.data_ptr() + 800, 90, to.data_ptr())
+    gpu.stream_check()
+    assert gpu.launch_count() - c0 == 1
+    items = [(ta.data_ptr(), 100, ta.data_ptr() + 800, 90, to.data_ptr()),
+             (ta.data_ptr(), 9000, ta.data_ptr() + 8 * 9000, 9000, to.data_ptr() + 8 * 200)]
+    b = gpu.Batch(items)
+    c0 = gpu.launch_count()
+    b.run()
+    b.run()
+    gpu.stream_check()
+    b.close()
+    assert gpu.launch_count() - c0 == 2 * (1 + 4)  # one single-CTA class, one four-step class

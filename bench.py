@@ -564,6 +564,59 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+FFT_N, FFT_SEEDS = 3000, (5, 6)
+
+
+def run_fft(args):
+    """The FP64 FFT band at 3000 x 3000 limbs (SplitMix64 seeds 5, 6): device
+    time per product through prec_gpu_mul_fft's kernels (operands resident:
+    timed by events around the host call's device part, reported by the
+    library), the digit width, the maximum rounding distance of the product,
+    and bit-exactness against the reference's mul_fft output (golden)."""
+    import torch
+
+    from preclib_gb300 import native, workloads
+    native.init(0)
+    a = workloads.operand(FFT_SEEDS[0], FFT_N)
+    b = workloads.operand(FFT_SEEDS[1], FFT_N)
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hb = torch.from_numpy(b.view(np.int64)).pin_memory()
+    ho = torch.empty(2 * FFT_N, dtype=torch.int64).pin_memory()
+    pa, pb, po = (x.numpy().view(np.uint64) for x in (ha, hb, ho))
+    L = native.lib()
+    for _ in range(args.warmup):
+        native.check(L.prec_gpu_mul_fft(native._p(pa), FFT_N, native._p(pb), FFT_N, native._p(po)))
+    dev_ms, e2e, dist = [], [], 0.0
+    launches0 = native.launch_count()
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            native.check(L.prec_gpu_mul_fft(native._p(pa), FFT_N, native._p(pb), FFT_N, native._p(po)))
+            e2e.append(time.perf_counter() - t)
+            st = native.last_stats()
+            dev_ms.append(st.device_ms)
+            dist = max(dist, st.fft_max_distance)
+    launches = native.launch_count() - launches0
+    with open(GOLDEN) as f:
+        want = [r for r in json.load(f)["products"] if r["name"] == "cfg2_3000x3000_fft"][0]
+    exact = hashlib.sha256(np.ascontiguousarray(po, dtype="<u8").tobytes()).hexdigest() == want["sha256"]
+    value = statistics.median(dev_ms)
+    line = {
+        "metric": "3000x3000-limb FP64 FFT-band mul ms", "value": round(value, 4), "unit": "ms", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "3000 x 3000-limb uint64 product (SplitMix64 seeds 5,6) on the FP64 FFT band",
+                   "digit_bits": native.fft_digit_bits(FFT_N, FFT_N), "transform_points": 1 << st.log2_n,
+                   "l2": "inputs (48 KB) fit L2; device time from the library's events"},
+        "max_rounding_distance": dist, "reference_max_rounding_distance": want.get("fft_max_err"),
+        "bit_exact": bool(exact),
+        "e2e": {"value": round(statistics.median(e2e) * 1e3, 4), "unit": "ms", "h2d_bytes_per_step": 16 * FFT_N,
+                "d2h_bytes_per_step": 16 * FFT_N},
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 PI_DIGITS = 100000000
 
 
@@ -624,9 +677,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="1m", choices=["1m", "batch", "serve", "pi"],
+    ap.add_argument("--workload", default="1m", choices=["1m", "batch", "serve", "pi", "fft"],
                     help="1m: the 1M x 1M product (default line); batch: 4096 uneven products; "
-                         "serve: serving loop under Poisson arrivals; pi: pi to 10^8 digits")
+                         "serve: serving loop under Poisson arrivals; pi: pi to 10^8 digits; "
+                         "fft: 3000 x 3000 limbs on the FP64 band")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
@@ -638,6 +692,8 @@ def main():
         run_serve(args)
     elif args.workload == "pi":
         run_pi(args)
+    elif args.workload == "fft":
+        run_fft(args)
     else:
         run_ours(args)
 

@@ -19,8 +19,9 @@
 //    k_fft_rows      rows k1 and N1-k1 together: row DIF, separation and
 //                    product (P_-k = conj P_k), row DIT, twiddle w^(i2 k1)
 //    k_fft_inv_cols  column DIT -> x/N -> nearest integer, max distance
-//    k_fft_carry     one CTA: limbs from the signed coefficients; writes
-//                    nothing when the max distance exceeds 0.25.
+//    k_fft_carry     limbs from the signed coefficients (blocks, then the
+//                    last block joins their carries); writes nothing when
+//                    the max distance exceeds 0.25.
 #include <cuda_runtime.h>
 
 #include "fft_kernels.cuh"
@@ -237,11 +238,37 @@ __device__ __forceinline__ int chain_step(uint64_t u, int g, int cin, uint64_t* 
     return g + fl;
 }
 
-__global__ void __launch_bounds__(1024) k_fft_carry(FftArgs f) {
-    __shared__ uint8_t maps[2][1024][3];
+// Carry maps {-1,0,1} -> {-1,0,1} packed as three 2-bit fields (value + 1).
+constexpr uint32_t kMapIdentity = 0u | (1u << 2) | (2u << 4);
+__device__ __forceinline__ int map_apply(uint32_t m, int x) { return (int)((m >> (2 * (x + 1))) & 3u) - 1; }
+// g after f
+__device__ __forceinline__ uint32_t map_compose(uint32_t g, uint32_t f) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int x = -1; x <= 1; ++x) r |= (uint32_t)(map_apply(g, map_apply(f, x)) + 1) << (2 * (x + 1));
+    return r;
+}
+
+constexpr int kFftCarryThreads = 256;
+constexpr int kFftCarryLimbs = 2;  // limbs per thread
+constexpr int kFftCarryBlockLimbs = kFftCarryThreads * kFftCarryLimbs;
+
+// Phase 1 (every block): the block's limbs from the signed coefficient sums,
+// the carry chain inside the block resolved with a block carry-in of 0
+// (maps composed by warp shuffles and a block scan), limbs written -- below
+// La+Lb to the output, above it to scratch -- and the block's composed map
+// published.  Phase 2 (the last block to finish, fence + atomic counter):
+// composes the block maps in order, adds each nonzero block carry-in into
+// its block (+1 ripples through all-ones limbs, -1 through zero limbs; rare),
+// and checks that every limb past La+Lb and the final carry are zero.
+// scratch (the transform buffer, free by now): [0] counter, [1 .. nblk]
+// block maps, then the limbs from La+Lb up.
+__global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(FftArgs f) {
+    __shared__ uint32_t s_wmap[kFftCarryThreads / 32];
+    __shared__ uint32_t s_last;
     const double dist = *f.maxdist;
-    if (!(dist <= 0.25)) {  // also NaN / inf
-        if (threadIdx.x == 0) atomicOr(f.err, kDevErrFftRound);
+    if (!(dist <= 0.25)) {  // also NaN / inf: nothing is written
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(f.err, kDevErrFftRound);
         return;
     }
     // Balanced digits can place signed contributions past the product's
@@ -250,50 +277,96 @@ __global__ void __launch_bounds__(1024) k_fft_carry(FftArgs f) {
     const int64_t Lout = (int64_t)f.lout;
     const int64_t Lcoef = (int64_t)(((uint64_t)f.b * f.ncoef + 63) / 64) + 2;
     const int64_t L = Lcoef > Lout ? Lcoef : Lout;
-    const int64_t per = (L + blockDim.x - 1) / blockDim.x;
-    const int64_t m0 = (int64_t)threadIdx.x * per;
-    const int64_t m1 = m0 + per < L ? m0 + per : L;
-    // this thread's chain as a map of the carry-in (index cin + 1)
-    int out_of[3];
-    for (int cin = -1; cin <= 1; ++cin) {
-        int c = cin;
+    const int nblk = (int)((L + kFftCarryBlockLimbs - 1) / kFftCarryBlockLimbs);
+    uint64_t* scr = reinterpret_cast<uint64_t*>(f.work);
+    uint32_t* counter = reinterpret_cast<uint32_t*>(scr);
+    uint64_t* bmap = scr + 1;
+    uint64_t* high = scr + 1 + nblk;  // limbs Lout .. L-1
+    auto limb_ref = [&](int64_t m) -> uint64_t& { return m < Lout ? f.out[m] : high[m - Lout]; };
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t m0 = (int64_t)blockIdx.x * kFftCarryBlockLimbs + (int64_t)threadIdx.x * kFftCarryLimbs;
+    uint64_t u[kFftCarryLimbs];
+    int g[kFftCarryLimbs];
+    {
         i128 prev = limb_sum_s(f.coef, f.ncoef, f.b, m0 - 1);
-        for (int64_t m = m0; m < m1; ++m) {
-            const i128 cur = limb_sum_s(f.coef, f.ncoef, f.b, m);
+#pragma unroll
+        for (int k = 0; k < kFftCarryLimbs; ++k) {
+            const i128 cur = m0 + k < L ? limb_sum_s(f.coef, f.ncoef, f.b, m0 + k) : (i128)0;
             const i128 v = (i128)(uint64_t)cur + (prev >> 64);
-            c = chain_step((uint64_t)v, (int)(v >> 64), c, nullptr);
+            u[k] = (uint64_t)v;
+            g[k] = (int)(v >> 64);
             prev = cur;
         }
-        out_of[cin + 1] = c < -1 ? -1 : (c > 1 ? 1 : c);
     }
-    int buf = 0;
-    for (int q = 0; q < 3; ++q) maps[0][threadIdx.x][q] = (uint8_t)(out_of[q] + 1);
+    // this thread's chain as a map of its carry-in
+    uint32_t tmap = 0;
+#pragma unroll
+    for (int x = -1; x <= 1; ++x) {
+        int c = x;
+#pragma unroll
+        for (int k = 0; k < kFftCarryLimbs; ++k)
+            if (m0 + k < L) c = chain_step(u[k], g[k], c, nullptr);
+        tmap |= (uint32_t)((c < -1 ? -1 : (c > 1 ? 1 : c)) + 1) << (2 * (x + 1));
+    }
+    // inclusive scan of the maps over the warp, then over the warps
+    uint32_t inc = tmap;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc = map_compose(inc, o);
+    }
+    if (lane == 31) s_wmap[warp] = inc;
     __syncthreads();
-    // inclusive scan of maps: M_t = f_t o f_{t-1} o ... o f_0
-    for (int d = 1; d < (int)blockDim.x; d <<= 1) {
-        uint8_t nm[3];
-        for (int q = 0; q < 3; ++q) {
-            const uint8_t mine = maps[buf][threadIdx.x][q];
-            nm[q] = mine;
-            if ((int)threadIdx.x >= d) nm[q] = maps[buf][threadIdx.x][maps[buf][threadIdx.x - d][q]];
+    uint32_t below = kMapIdentity;  // warps before this one
+    for (int w = 0; w < warp; ++w) below = map_compose(s_wmap[w], below);
+    uint32_t excl = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) excl = kMapIdentity;
+    const int cin = map_apply(map_compose(excl, below), 0);
+    {
+        int c = cin;
+#pragma unroll
+        for (int k = 0; k < kFftCarryLimbs; ++k) {
+            if (m0 + k >= L) break;
+            uint64_t limb;
+            c = chain_step(u[k], g[k], c, &limb);
+            limb_ref(m0 + k) = limb;
         }
-        for (int q = 0; q < 3; ++q) maps[buf ^ 1][threadIdx.x][q] = nm[q];
-        __syncthreads();
-        buf ^= 1;
     }
-    // carry into this thread's first limb: prefix map of threads < t applied to 0
-    int c = threadIdx.x == 0 ? 0 : (int)maps[buf][threadIdx.x - 1][1] - 1;
-    i128 prev = limb_sum_s(f.coef, f.ncoef, f.b, m0 - 1);
-    for (int64_t m = m0; m < m1; ++m) {
-        const i128 cur = limb_sum_s(f.coef, f.ncoef, f.b, m);
-        const i128 v = (i128)(uint64_t)cur + (prev >> 64);
-        uint64_t limb;
-        c = chain_step((uint64_t)v, (int)(v >> 64), c, &limb);
-        if (m < Lout) f.out[m] = limb;
-        else if (limb != 0) atomicOr(f.err, kDevErrCarry);  // a product fits La+Lb limbs
-        prev = cur;
+    if (threadIdx.x == 0) {
+        uint32_t bm = kMapIdentity;
+        for (int w = 0; w < kFftCarryThreads / 32; ++w) bm = map_compose(s_wmap[w], bm);
+        bmap[blockIdx.x] = bm;
     }
-    if (m0 < L && m1 == L && c != 0) atomicOr(f.err, kDevErrCarry);
+    // ---- phase 2: the last block resolves the carries between blocks
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == (uint32_t)gridDim.x - 1 ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int bk = 0; bk < nblk; ++bk) {
+            if (c != 0) {
+                const int64_t e = (int64_t)(bk + 1) * kFftCarryBlockLimbs < L ? (int64_t)(bk + 1) * kFftCarryBlockLimbs : L;
+                for (int64_t m = (int64_t)bk * kFftCarryBlockLimbs; m < e; ++m) {
+                    uint64_t& x = limb_ref(m);
+                    const uint64_t old = __ldcg(&x);
+                    x = old + (uint64_t)(int64_t)c;
+                    if (c > 0 ? old != ~0ull : old != 0) break;
+                }
+            }
+            c = map_apply((uint32_t)__ldcg(&bmap[bk]), c);
+        }
+        if (c != 0) atomicOr(f.err, kDevErrCarry);
+    }
+    __syncthreads();
+    // a product fits La+Lb limbs: everything above must be zero
+    for (int64_t m = Lout + threadIdx.x; m < L; m += blockDim.x)
+        if (__ldcg(&high[m - Lout]) != 0) atomicOr(f.err, kDevErrCarry);
 }
 
 // e^(2 pi i e / 2^16) for e < 2^15
@@ -340,7 +413,13 @@ void fft_launch(const FftArgs& f, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[2], st);
     k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
     if (ev) cudaEventRecord(ev[3], st);
-    k_fft_carry<<<1, 1024, 0, st>>>(f);
+    {
+        const int64_t lcoef = (int64_t)(((uint64_t)f.b * f.ncoef + 63) / 64) + 2;
+        const int64_t L = lcoef > (int64_t)f.lout ? lcoef : (int64_t)f.lout;
+        const int nblk = (int)((L + kFftCarryBlockLimbs - 1) / kFftCarryBlockLimbs);
+        cudaMemsetAsync(f.work, 0, sizeof(uint64_t), st);  // the carry kernel's counter
+        k_fft_carry<<<nblk, kFftCarryThreads, 0, st>>>(f);
+    }
     count_launches(4);
     if (ev) cudaEventRecord(ev[4], st);
 }

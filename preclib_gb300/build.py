@@ -65,7 +65,7 @@ def build(verbose: bool = False, extra=()) -> str:
     return out
 
 
-PI_SOURCES = ("bignum.cpp", "pi_chudnovsky.cpp")
+PI_SOURCES = ("bignum.cpp", "pi_chudnovsky.cpp", "pi_kernels.cu")
 PI_EXE = "pi_gb300"
 
 
@@ -73,8 +73,9 @@ def build_pi() -> str:
     """The pi program (pi/*.cpp, host C++) linked against lib/libprecgpu.so."""
     srcs = [os.path.join(PKG, "pi", f) for f in PI_SOURCES]
     out = os.path.join(LIBDIR, PI_EXE)
-    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-pthread", "-I", os.path.join(PKG, "..", "include"),
-           *srcs, "-L", LIBDIR, "-lprecgpu", "-Xlinker", "-rpath=" + LIBDIR, "-o", out + ".tmp"]
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-pthread",
+           "-I", os.path.join(PKG, "..", "include"), *srcs, "-L", LIBDIR, "-lprecgpu",
+           "-Xlinker", "-rpath=" + LIBDIR, "-o", out + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("pi program build failed:\n%s%s" % (r.stdout, r.stderr))

@@ -156,17 +156,24 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
             b->zero_items.push_back((int)i);
             continue;
         }
-        Plan pl;
-        if ((r = plan_for(2 * (uint64_t)p.an, 2 * (uint64_t)p.bn, p.an + p.bn, pl))) {
+        // the transform length alone picks the class; the class plan (CRT
+        // constants, kernel configuration) is made once, for its first product
+        const uint64_t need = 2 * (uint64_t)p.an + 2 * (uint64_t)p.bn - 1;
+        int k = kSmallMinLog2;
+        while ((1ull << k) < need) ++k;
+        if (k > kSetMaxLog2[kSets - 1]) {
             batch_free(b);
-            return r;
+            return PREC_GPU_E_TOO_LARGE;
         }
-        const int sq = (p.a == p.b && p.an == p.bn && pl.path == 1) ? 1 : 0;
-        Cls& c = by_k[2 * pl.k + sq];
+        const int sq = (p.a == p.b && p.an == p.bn && k > kSmallMaxLog2) ? 1 : 0;
+        Cls& c = by_k[2 * k + sq];
         if (c.items.empty()) {
-            c.k = pl.k;
+            if ((r = plan_for(2 * (uint64_t)p.an, 2 * (uint64_t)p.bn, p.an + p.bn, c.pl))) {
+                batch_free(b);
+                return r;
+            }
+            c.k = c.pl.k;
             c.square = sq;
-            c.pl = pl;
         }
         c.items.push_back((int)i);
     }

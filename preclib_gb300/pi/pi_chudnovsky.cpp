@@ -33,6 +33,7 @@
 
 #include "../../include/prec_gpu.h"
 #include "bignum.hpp"
+#include "pi_device.hpp"
 
 using namespace precpi;
 
@@ -264,6 +265,192 @@ bool trace_on() {
     return on;
 }
 
+// ---------------------------------------------------------------------------
+// binary splitting with the levels resident in device memory
+// ---------------------------------------------------------------------------
+
+// One level of the tree on the device: P, Q and |T| of every node in one
+// buffer (offsets in limbs, 4-limb aligned), T's signs in another.
+struct DevLevel {
+    std::vector<uint64_t> op, oq, ot;
+    std::vector<uint32_t> np, nq, nt;
+    uint64_t* buf = nullptr;
+    int8_t* sign = nullptr;
+    size_t nodes() const { return nq.size(); }
+    void release() {
+        if (buf) cudaFree(buf);
+        if (sign) cudaFree(sign);
+        buf = nullptr;
+        sign = nullptr;
+    }
+};
+
+size_t up4(size_t x) { return (x + 3) & ~(size_t)3; }
+
+template <class T>
+T* dev_alloc(size_t n) {
+    void* p = nullptr;
+    check_cuda(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "device level buffer");
+    return static_cast<T*>(p);
+}
+
+// the bottom level, from host-computed nodes
+void upload_level(const std::vector<Node>& nodes, DevLevel& L, cudaStream_t st) {
+    const size_t m = nodes.size();
+    L.op.resize(m), L.oq.resize(m), L.ot.resize(m), L.np.resize(m), L.nq.resize(m), L.nt.resize(m);
+    size_t total = 0;
+    for (size_t i = 0; i < m; ++i) {
+        L.np[i] = (uint32_t)nodes[i].p.size(), L.nq[i] = (uint32_t)nodes[i].q.size(), L.nt[i] = (uint32_t)nodes[i].t.size();
+        L.op[i] = total, total += up4(L.np[i]);
+        L.oq[i] = total, total += up4(L.nq[i]);
+        L.ot[i] = total, total += up4(L.nt[i]);
+    }
+    u64* h = nullptr;
+    int8_t* hs = nullptr;
+    check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&h), std::max<size_t>(total, 1) * sizeof(u64), 0), "pinned level");
+    check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&hs), std::max<size_t>(m, 1), 0), "pinned signs");
+    parallel_for(m, [&](size_t i) {
+        std::copy(nodes[i].p.d.begin(), nodes[i].p.d.end(), h + L.op[i]);
+        std::copy(nodes[i].q.d.begin(), nodes[i].q.d.end(), h + L.oq[i]);
+        std::copy(nodes[i].t.d.begin(), nodes[i].t.d.end(), h + L.ot[i]);
+        hs[i] = nodes[i].neg ? 1 : 0;
+    });
+    L.buf = dev_alloc<u64>(total);
+    L.sign = dev_alloc<int8_t>(m);
+    check_cuda(cudaMemcpyAsync(L.buf, h, total * sizeof(u64), cudaMemcpyHostToDevice, st), "level upload");
+    check_cuda(cudaMemcpyAsync(L.sign, hs, m, cudaMemcpyHostToDevice, st), "sign upload");
+    check_cuda(cudaStreamSynchronize(st), "level upload");
+    cudaFreeHost(h);
+    cudaFreeHost(hs);
+}
+
+Nat download(const uint64_t* d, size_t n, cudaStream_t st) {
+    Nat r;
+    r.d.resize(n);
+    check_cuda(cudaMemcpyAsync(r.d.data(), d, n * sizeof(u64), cudaMemcpyDeviceToHost, st), "download");
+    check_cuda(cudaStreamSynchronize(st), "download");
+    normalize(r);
+    return r;
+}
+
+bool trace_on();
+Node host_split(u64 a, u64 b);
+
+// Q(0, terms) and T(0, terms): host blocks of 16 terms, then every level on
+// the device (products through one batch per level, T's signed sums by
+// signed_add_many); only the root comes back.
+void binary_split_device(size_t terms, Nat& Q, Nat& T, bool& tneg) {
+    constexpr size_t kHostBlock = 16;
+    cudaStream_t st;
+    check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+    double t0 = now_sec();
+    DevLevel cur;
+    {
+        std::vector<Node> nodes((terms + kHostBlock - 1) / kHostBlock);
+        parallel_for(nodes.size(), [&](size_t i) {
+            nodes[i] = host_split(i * kHostBlock, std::min<size_t>(terms, (i + 1) * kHostBlock));
+        });
+        upload_level(nodes, cur, st);
+    }
+    if (trace_on()) std::fprintf(stderr, "  blocks of %zu terms: %zu nodes on the device %.3f s\n", kHostBlock,
+                                 cur.nodes(), now_sec() - t0);
+    std::vector<prec_gpu_product_t> items;
+    std::vector<AddPair> pairs;
+    std::vector<uint32_t> chunk_pair;
+    while (cur.nodes() > 1) {
+        t0 = now_sec();
+        const size_t m = cur.nodes(), npair = m / 2;
+        const bool last_pair_is_last = (m % 2) == 0;
+        DevLevel nx;
+        const size_t mn = (m + 1) / 2;
+        nx.op.resize(mn), nx.oq.resize(mn), nx.ot.resize(mn), nx.np.resize(mn), nx.nq.resize(mn), nx.nt.resize(mn);
+        std::vector<uint64_t> o1(npair), o2(npair);
+        std::vector<uint32_t> n1(npair), n2(npair);
+        size_t total = 0, tmp = 0;
+        for (size_t i = 0; i < npair; ++i) {
+            const size_t l = 2 * i, r = 2 * i + 1;
+            const bool need_p = !(last_pair_is_last && i == npair - 1);
+            n1[i] = cur.nt[l] + cur.nq[r];
+            n2[i] = cur.nt[r] + cur.np[l];
+            nx.np[i] = need_p ? cur.np[l] + cur.np[r] : 0;
+            nx.nq[i] = cur.nq[l] + cur.nq[r];
+            nx.nt[i] = std::max(n1[i], n2[i]) + 1;
+            nx.op[i] = total, total += up4(nx.np[i]);
+            nx.oq[i] = total, total += up4(nx.nq[i]);
+            nx.ot[i] = total, total += up4(nx.nt[i]);
+            o1[i] = tmp, tmp += up4(n1[i]);
+            o2[i] = tmp, tmp += up4(n2[i]);
+        }
+        if (m % 2) {  // the last node moves up unchanged
+            const size_t s = m - 1, d = mn - 1;
+            nx.np[d] = cur.np[s], nx.nq[d] = cur.nq[s], nx.nt[d] = cur.nt[s];
+            nx.op[d] = total, total += up4(nx.np[d]);
+            nx.oq[d] = total, total += up4(nx.nq[d]);
+            nx.ot[d] = total, total += up4(nx.nt[d]);
+        }
+        nx.buf = dev_alloc<u64>(total);
+        nx.sign = dev_alloc<int8_t>(mn);
+        uint64_t* tbuf = dev_alloc<u64>(tmp);
+        items.clear();
+        for (size_t i = 0; i < npair; ++i) {
+            const size_t l = 2 * i, r = 2 * i + 1;
+            auto P = [&](uint64_t off) { return cur.buf + off; };
+            items.push_back({P(cur.oq[l]), cur.nq[l], P(cur.oq[r]), cur.nq[r], nx.buf + nx.oq[i]});
+            items.push_back({P(cur.ot[l]), cur.nt[l], P(cur.oq[r]), cur.nq[r], tbuf + o1[i]});
+            items.push_back({P(cur.ot[r]), cur.nt[r], P(cur.op[l]), cur.np[l], tbuf + o2[i]});
+            if (nx.np[i]) items.push_back({P(cur.op[l]), cur.np[l], P(cur.op[r]), cur.np[r], nx.buf + nx.op[i]});
+        }
+        int rc = prec_gpu_mul_batch(items.data(), items.size(), st);
+        if (rc) die("prec_gpu_mul_batch", rc);
+        pairs.resize(npair);
+        chunk_pair.clear();
+        for (size_t i = 0; i < npair; ++i) {
+            AddPair& a = pairs[i];
+            a.x = tbuf + o1[i];
+            a.y = tbuf + o2[i];
+            a.z = nx.buf + nx.ot[i];
+            a.sx = cur.sign + 2 * i;
+            a.sy = cur.sign + 2 * i + 1;
+            a.sz = nx.sign + i;
+            a.nx = n1[i], a.ny = n2[i], a.nz = nx.nt[i];
+            a.chunk0 = (uint32_t)chunk_pair.size();
+            chunk_pair.insert(chunk_pair.end(), add_chunks(a.nz), (uint32_t)i);
+        }
+        AddPair* d_pairs = dev_alloc<AddPair>(npair);
+        uint32_t* d_chunks = dev_alloc<uint32_t>(chunk_pair.size());
+        void* scratch = dev_alloc<uint8_t>(signed_add_scratch_bytes(npair, chunk_pair.size()));
+        check_cuda(cudaMemcpyAsync(d_pairs, pairs.data(), npair * sizeof(AddPair), cudaMemcpyHostToDevice, st), "pairs");
+        check_cuda(cudaMemcpyAsync(d_chunks, chunk_pair.data(), chunk_pair.size() * sizeof(uint32_t),
+                                   cudaMemcpyHostToDevice, st), "chunks");
+        check_cuda(signed_add_many(d_pairs, npair, d_chunks, chunk_pair.size(), scratch, st), "signed sums");
+        if (m % 2) {
+            const size_t s = m - 1, d = mn - 1;
+            if (cur.np[s])
+                cudaMemcpyAsync(nx.buf + nx.op[d], cur.buf + cur.op[s], cur.np[s] * sizeof(u64), cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(nx.buf + nx.oq[d], cur.buf + cur.oq[s], cur.nq[s] * sizeof(u64), cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(nx.buf + nx.ot[d], cur.buf + cur.ot[s], cur.nt[s] * sizeof(u64), cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(nx.sign + d, cur.sign + s, 1, cudaMemcpyDeviceToDevice, st);
+        }
+        check_cuda(cudaStreamSynchronize(st), "level");
+        cudaFree(d_pairs);
+        cudaFree(d_chunks);
+        cudaFree(scratch);
+        cudaFree(tbuf);
+        cur.release();
+        cur = std::move(nx);
+        if (trace_on())
+            std::fprintf(stderr, "  level of %zu nodes on the device: %zu products, Q of the first node %u limbs, %.3f s\n",
+                         m, items.size(), cur.nq[0], now_sec() - t0);
+    }
+    Q = download(cur.buf + cur.oq[0], cur.nq[0], st);
+    T = download(cur.buf + cur.ot[0], cur.nt[0], st);
+    int8_t sg = 0;
+    check_cuda(cudaMemcpy(&sg, cur.sign, 1, cudaMemcpyDeviceToHost), "sign");
+    tneg = sg != 0;
+    cur.release();
+    cudaStreamDestroy(st);
+}
+
 // Q(0, terms) and T(0, terms)
 void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
     // the lowest levels in blocks of kHostBlock terms on the host threads:
@@ -326,7 +513,10 @@ std::string pi_digits(size_t digits, Phases& ph) {
     double t0 = now_sec();
     Nat Q, T;
     bool tneg = false;
-    binary_split(terms, Q, T, tneg);
+    // PI_GB300_HOST_LEVELS=1: the tree's levels on the host, products staged
+    // through host memory per level (the slower form, for comparison)
+    if (std::getenv("PI_GB300_HOST_LEVELS")) binary_split(terms, Q, T, tneg);
+    else binary_split_device(terms, Q, T, tneg);
     double t1 = now_sec();
     if (tneg || T.zero()) return "error";
     const Nat n = mul_u64(pow_u64(10, 2 * work), 10005);
@@ -395,7 +585,8 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu\n", be.gpu_products,
                      be.host_products, be.batches);
     }
-    std::fprintf(stderr, "gpu_launches %llu\n", (unsigned long long)prec_gpu_launch_count());
+    std::fprintf(stderr, "gpu_launches %llu\n",
+                 (unsigned long long)(prec_gpu_launch_count() + signed_add_launches()));
     if (!file.empty()) std::fprintf(stderr, "wrote %s\n", file.c_str());
     std::fprintf(stderr, "time %.6f sec\n", sec);
     return 0;

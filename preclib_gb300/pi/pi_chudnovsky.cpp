@@ -305,10 +305,12 @@ void upload_level(const std::vector<Node>& nodes, DevLevel& L, cudaStream_t st) 
         L.oq[i] = total, total += up4(L.nq[i]);
         L.ot[i] = total, total += up4(L.nt[i]);
     }
-    u64* h = nullptr;
-    int8_t* hs = nullptr;
-    check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&h), std::max<size_t>(total, 1) * sizeof(u64), 0), "pinned level");
-    check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&hs), std::max<size_t>(m, 1), 0), "pinned signs");
+    // one ordinary host buffer: page-locking a buffer this size costs more
+    // than the staged copy it would save
+    std::vector<u64> hv(std::max<size_t>(total, 1));
+    std::vector<int8_t> hsv(std::max<size_t>(m, 1));
+    u64* h = hv.data();
+    int8_t* hs = hsv.data();
     parallel_for(m, [&](size_t i) {
         std::copy(nodes[i].p.d.begin(), nodes[i].p.d.end(), h + L.op[i]);
         std::copy(nodes[i].q.d.begin(), nodes[i].q.d.end(), h + L.oq[i]);
@@ -320,8 +322,6 @@ void upload_level(const std::vector<Node>& nodes, DevLevel& L, cudaStream_t st) 
     check_cuda(cudaMemcpyAsync(L.buf, h, total * sizeof(u64), cudaMemcpyHostToDevice, st), "level upload");
     check_cuda(cudaMemcpyAsync(L.sign, hs, m, cudaMemcpyHostToDevice, st), "sign upload");
     check_cuda(cudaStreamSynchronize(st), "level upload");
-    cudaFreeHost(h);
-    cudaFreeHost(hs);
 }
 
 Nat download(const uint64_t* d, size_t n, cudaStream_t st) {

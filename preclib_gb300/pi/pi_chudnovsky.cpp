@@ -294,33 +294,132 @@ T* dev_alloc(size_t n) {
     return static_cast<T*>(p);
 }
 
-// the bottom level, from host-computed nodes
-void upload_level(const std::vector<Node>& nodes, DevLevel& L, cudaStream_t st) {
-    const size_t m = nodes.size();
-    L.op.resize(m), L.oq.resize(m), L.ot.resize(m), L.np.resize(m), L.nq.resize(m), L.nt.resize(m);
-    size_t total = 0;
-    for (size_t i = 0; i < m; ++i) {
-        L.np[i] = (uint32_t)nodes[i].p.size(), L.nq[i] = (uint32_t)nodes[i].q.size(), L.nt[i] = (uint32_t)nodes[i].t.size();
-        L.op[i] = total, total += up4(L.np[i]);
-        L.oq[i] = total, total += up4(L.nq[i]);
-        L.ot[i] = total, total += up4(L.nt[i]);
+// A 16-term block on the stack: the node of terms [a, b) with fixed-size
+// magnitudes (no heap allocation), by the same recursive halving.
+constexpr int kSmallLimbs = 48;  // bound of P, Q, |T| of 16 terms (about 36 limbs)
+
+struct SmallNat {
+    uint32_t n = 0;
+    u64 d[kSmallLimbs];
+};
+struct SmallNode {
+    SmallNat p, q, t;
+    bool neg = false;
+};
+
+void small_set(SmallNat& x, u128 v) {
+    x.d[0] = (u64)v;
+    x.d[1] = (u64)(v >> 64);
+    x.n = x.d[1] ? 2 : (x.d[0] ? 1 : 0);
+}
+
+void small_mul(const SmallNat& a, const SmallNat& b, SmallNat& r) {
+    if (!a.n || !b.n) {
+        r.n = 0;
+        return;
     }
-    // one ordinary host buffer: page-locking a buffer this size costs more
-    // than the staged copy it would save
-    std::vector<u64> hv(std::max<size_t>(total, 1));
-    std::vector<int8_t> hsv(std::max<size_t>(m, 1));
-    u64* h = hv.data();
-    int8_t* hs = hsv.data();
+    if (a.n + b.n > (uint32_t)kSmallLimbs) std::abort();
+    mul_school(a.d, a.n, b.d, b.n, r.d);
+    r.n = a.n + b.n;
+    while (r.n && r.d[r.n - 1] == 0) --r.n;
+}
+
+int small_cmp(const SmallNat& a, const SmallNat& b) {
+    if (a.n != b.n) return a.n < b.n ? -1 : 1;
+    for (uint32_t i = a.n; i-- > 0;)
+        if (a.d[i] != b.d[i]) return a.d[i] < b.d[i] ? -1 : 1;
+    return 0;
+}
+
+// r = a + b or |a - b| with its sign, as signed_add
+void small_signed_add(const SmallNat& a, bool an, const SmallNat& b, bool bn, SmallNat& r, bool& rn) {
+    if (an == bn) {
+        const SmallNat& x = a.n >= b.n ? a : b;
+        const SmallNat& y = a.n >= b.n ? b : a;
+        u64 c = 0;
+        for (uint32_t i = 0; i < x.n; ++i) {
+            const u128 s = (u128)x.d[i] + (i < y.n ? y.d[i] : 0) + c;
+            r.d[i] = (u64)s;
+            c = (u64)(s >> 64);
+        }
+        r.n = x.n;
+        if (c) {
+            if (r.n >= (uint32_t)kSmallLimbs) std::abort();
+            r.d[r.n++] = c;
+        }
+        rn = an && r.n;
+        return;
+    }
+    const bool a_big = small_cmp(a, b) >= 0;
+    const SmallNat& x = a_big ? a : b;
+    const SmallNat& y = a_big ? b : a;
+    u64 br = 0;
+    for (uint32_t i = 0; i < x.n; ++i) {
+        const u64 yi = i < y.n ? y.d[i] : 0;
+        const u64 t = x.d[i] - yi - br;
+        br = (x.d[i] < yi) || (x.d[i] == yi && br) ? 1 : 0;
+        r.d[i] = t;
+    }
+    r.n = x.n;
+    while (r.n && r.d[r.n - 1] == 0) --r.n;
+    rn = (a_big ? an : bn) && r.n;
+}
+
+void small_leaf(u64 k, SmallNode& n) {
+    if (k == 0) {
+        small_set(n.p, 1);
+        small_set(n.q, 1);
+        small_set(n.t, kA);
+        n.neg = false;
+        return;
+    }
+    const u128 p = (u128)(6 * k - 5) * (2 * k - 1) * (6 * k - 1);
+    small_set(n.p, p);
+    small_set(n.q, (u128)k * k * k * kC3Over24);
+    small_set(n.t, p * (u128)(kB * k + kA));
+    n.neg = (k & 1) != 0;
+}
+
+void small_split(u64 a, u64 b, SmallNode& out) {
+    if (b - a == 1) {
+        small_leaf(a, out);
+        return;
+    }
+    const u64 m = a + (b - a) / 2;
+    SmallNode l, r;
+    small_split(a, m, l);
+    small_split(m, b, r);
+    SmallNat t1, t2;
+    small_mul(l.q, r.q, out.q);
+    small_mul(l.t, r.q, t1);
+    small_mul(r.t, l.p, t2);
+    small_mul(l.p, r.p, out.p);
+    small_signed_add(t1, l.neg, t2, r.neg, out.t, out.neg);
+}
+
+// the bottom level (blocks of `block` terms) computed on the host threads
+// straight into fixed slots of the upload buffer
+void upload_blocks(size_t terms, size_t block, DevLevel& L, cudaStream_t st) {
+    const size_t m = (terms + block - 1) / block;
+    constexpr size_t slot = 3 * kSmallLimbs;
+    L.op.resize(m), L.oq.resize(m), L.ot.resize(m), L.np.resize(m), L.nq.resize(m), L.nt.resize(m);
+    std::vector<u64> hv(m * slot);
+    std::vector<int8_t> hs(m);
     parallel_for(m, [&](size_t i) {
-        std::copy(nodes[i].p.d.begin(), nodes[i].p.d.end(), h + L.op[i]);
-        std::copy(nodes[i].q.d.begin(), nodes[i].q.d.end(), h + L.oq[i]);
-        std::copy(nodes[i].t.d.begin(), nodes[i].t.d.end(), h + L.ot[i]);
-        hs[i] = nodes[i].neg ? 1 : 0;
+        SmallNode nd;
+        small_split(i * block, std::min<size_t>(terms, (i + 1) * block), nd);
+        u64* h = hv.data() + i * slot;
+        std::copy(nd.p.d, nd.p.d + nd.p.n, h);
+        std::copy(nd.q.d, nd.q.d + nd.q.n, h + kSmallLimbs);
+        std::copy(nd.t.d, nd.t.d + nd.t.n, h + 2 * kSmallLimbs);
+        L.op[i] = i * slot, L.oq[i] = i * slot + kSmallLimbs, L.ot[i] = i * slot + 2 * kSmallLimbs;
+        L.np[i] = nd.p.n, L.nq[i] = nd.q.n, L.nt[i] = nd.t.n;
+        hs[i] = nd.neg ? 1 : 0;
     });
-    L.buf = dev_alloc<u64>(total);
+    L.buf = dev_alloc<u64>(hv.size());
     L.sign = dev_alloc<int8_t>(m);
-    check_cuda(cudaMemcpyAsync(L.buf, h, total * sizeof(u64), cudaMemcpyHostToDevice, st), "level upload");
-    check_cuda(cudaMemcpyAsync(L.sign, hs, m, cudaMemcpyHostToDevice, st), "sign upload");
+    check_cuda(cudaMemcpyAsync(L.buf, hv.data(), hv.size() * sizeof(u64), cudaMemcpyHostToDevice, st), "level upload");
+    check_cuda(cudaMemcpyAsync(L.sign, hs.data(), m, cudaMemcpyHostToDevice, st), "sign upload");
     check_cuda(cudaStreamSynchronize(st), "level upload");
 }
 
@@ -345,13 +444,7 @@ void binary_split_device(size_t terms, Nat& Q, Nat& T, bool& tneg) {
     check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
     double t0 = now_sec();
     DevLevel cur;
-    {
-        std::vector<Node> nodes((terms + kHostBlock - 1) / kHostBlock);
-        parallel_for(nodes.size(), [&](size_t i) {
-            nodes[i] = host_split(i * kHostBlock, std::min<size_t>(terms, (i + 1) * kHostBlock));
-        });
-        upload_level(nodes, cur, st);
-    }
+    upload_blocks(terms, kHostBlock, cur, st);
     if (trace_on()) std::fprintf(stderr, "  blocks of %zu terms: %zu nodes on the device %.3f s\n", kHostBlock,
                                  cur.nodes(), now_sec() - t0);
     std::vector<prec_gpu_product_t> items;

@@ -67,6 +67,8 @@ struct prec_gpu_batch {
     std::vector<int> zero_items;  // products with a zero-length operand
     void* d_mem = nullptr;
     size_t d_bytes = 0;
+    cudaStream_t oneshot = nullptr;  // one-shot form: d_mem from the library pool on this stream
+    bool pooled = false;
     cudaStream_t cap = nullptr;
     cudaEvent_t fork = nullptr;
     cudaGraph_t graph = nullptr;
@@ -85,7 +87,10 @@ static void batch_free(prec_gpu_batch* b) {
     }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->cap) cudaStreamDestroy(b->cap);
-    if (b->d_mem) cudaFree(b->d_mem);
+    if (b->d_mem) {
+        if (b->pooled) cudaFreeAsync(b->d_mem, b->oneshot);
+        else cudaFree(b->d_mem);
+    }
     delete b;
 }
 
@@ -134,15 +139,19 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
     }
 }
 
-extern "C" {
-
-int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gpu_batch_t** out) {
+// Plans a batch and uploads its descriptors.  `oneshot` (prec_gpu_mul_batch):
+// the device memory comes stream-ordered from the library pool on that
+// stream (no device-wide allocation or free per call), and no stream
+// branches or capture stream are made.
+static int batch_build(const prec_gpu_product_t* items, size_t count, bool oneshot, cudaStream_t ost,
+                       prec_gpu_batch** out) {
     if (!out || (!items && count)) return PREC_GPU_E_ARG;
     *out = nullptr;
     std::lock_guard<std::mutex> lk(ctx_mutex());
     int r = ctx_init_locked(-1);
     if (r) return r;
     prec_gpu_batch* b = new prec_gpu_batch();
+    b->oneshot = ost;
     b->items.assign(items, items + count);
     b->err = ctx_device_err();
     std::map<int, Cls> by_k;  // key 2k + square
@@ -198,7 +207,16 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
         b->classes.push_back(c);
     }
     b->d_bytes = bytes;
-    if (bytes) BCK(cudaMalloc(&b->d_mem, bytes));
+    if (bytes && oneshot) {
+        BCK(cudaMallocFromPoolAsync(&b->d_mem, bytes, ctx_pool(), ost));
+        b->pooled = true;
+    } else if (bytes) {
+        BCK(cudaMalloc(&b->d_mem, bytes));
+    }
+    auto upload = [&](void* dst, const void* src, size_t n) {
+        return oneshot ? cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, ost)
+                       : cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
+    };
     uint8_t* base = static_cast<uint8_t*>(b->d_mem);
     for (size_t ci = 0; ci < b->classes.size(); ++ci) {
         Cls& c = b->classes[ci];
@@ -219,7 +237,7 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
                 d.crt = c.pl.crt;
             }
             c.d_small = reinterpret_cast<SmallDesc*>(base + desc_off[ci]);
-            BCK(cudaMemcpy(c.d_small, h.data(), n * sizeof(SmallDesc), cudaMemcpyHostToDevice));
+            BCK(upload(c.d_small, h.data(), n * sizeof(SmallDesc)));
         } else {
             c.ws = base + ws_off[ci];
             std::vector<ProdPtrs> h(n);
@@ -247,15 +265,24 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
                 c.chunks.push_back(ch);
             }
             c.d_ptrs = reinterpret_cast<ProdPtrs*>(base + desc_off[ci]);
-            BCK(cudaMemcpy(c.d_ptrs, h.data(), n * sizeof(ProdPtrs), cudaMemcpyHostToDevice));
+            BCK(upload(c.d_ptrs, h.data(), n * sizeof(ProdPtrs)));
         }
+        if (oneshot) continue;
         BCK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
         BCK(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
     }
-    BCK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
-    BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    if (!oneshot) {
+        BCK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+        BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    }
     *out = b;
     return PREC_GPU_OK;
+}
+
+extern "C" {
+
+int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gpu_batch_t** out) {
+    return batch_build(items, count, false, nullptr, out);
 }
 
 int prec_gpu_batch_run(prec_gpu_batch_t* b, void* stream) {
@@ -292,14 +319,14 @@ void prec_gpu_batch_destroy(prec_gpu_batch_t* b) {
 }
 
 int prec_gpu_mul_batch(const prec_gpu_product_t* items, size_t count, void* stream) {
-    prec_gpu_batch_t* b = nullptr;
-    int r = prec_gpu_batch_create(items, count, &b);
-    if (r) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    prec_gpu_batch_t* b = nullptr;
+    int r = batch_build(items, count, true, st, &b);
+    if (r) return r;
     batch_enqueue(b, st, false);
     cudaError_t e = cudaGetLastError();
+    batch_free(b);  // the workspace returns to the pool after the batch's work on `st`
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    batch_free(b);
     return cuda_code(e);
 }
 

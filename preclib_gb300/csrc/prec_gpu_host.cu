@@ -153,6 +153,7 @@ struct Ctx {
     cudaEvent_t stage_ev[kMaxStages + 1] = {};
     FieldArgs field[kSets] = {};
     PrimeStreams prime_streams = {};
+    cudaMemPool_t pool = nullptr;
     bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
 };
 
@@ -271,6 +272,15 @@ static int init_locked(Ctx& c, int device) {
     }
     CK(cudaEventCreateWithFlags(&c.prime_streams.fork, cudaEventDisableTiming));
     {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        CK(cudaMemPoolCreate(&c.pool, &props));
+        uint64_t keep = ~0ull;
+        CK(cudaMemPoolSetAttribute(c.pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+    {
         const char* env = std::getenv("PREC_GPU_PRIME_STREAMS");
         c.split_primes = !(env && env[0] == '0');
     }
@@ -299,6 +309,7 @@ std::mutex& ctx_mutex() { return g_ctx.mu; }
 int ctx_init_locked(int device) { return init_locked(g_ctx, device); }
 const FieldArgs& ctx_field(int set) { return g_ctx.field[set]; }
 int* ctx_device_err() { return g_ctx.d_err; }
+cudaMemPool_t ctx_pool() { return g_ctx.pool; }
 
 static int ensure_ws(Ctx& c, size_t bytes) {
     if (bytes <= c.ws_cap) return 0;
@@ -582,6 +593,8 @@ void prec_gpu_shutdown(void) {
     }
     cudaEventDestroy(c.prime_streams.fork);
     c.prime_streams = PrimeStreams{};
+    if (c.pool) cudaMemPoolDestroy(c.pool);
+    c.pool = nullptr;
     cudaStreamDestroy(c.stream);
     c.ws = nullptr;
     c.io = nullptr;

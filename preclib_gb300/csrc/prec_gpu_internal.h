@@ -62,6 +62,9 @@ std::mutex& ctx_mutex();
 int ctx_init_locked(int device);
 const FieldArgs& ctx_field(int set);
 int* ctx_device_err();
+// the library's stream-ordered memory pool (freed memory stays resident):
+// workspace of one-shot batches
+cudaMemPool_t ctx_pool();
 
 int cuda_code(cudaError_t e);
 

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -388,7 +389,13 @@ void leaf_digits(Nat v, char* out) {
 
 }  // namespace
 
+static double tnow() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 std::string to_decimal(const Nat& x, size_t width) {
+    static const bool trace = std::getenv("PI_GB300_TRACE") != nullptr;
+    double t0 = tnow();
     // digits of x are at most floor(bitlen * log10(2)) + 1
     const size_t need = std::max<size_t>(width, (size_t)((double)bitlen(x) * 0.30102999566398120) + 2);
     int J = 0;
@@ -397,11 +404,14 @@ std::string to_decimal(const Nat& x, size_t width) {
     std::vector<Nat> pw(J > 0 ? J : 0);
     if (J > 0) pw[0] = pow_u64(10, kLeafDigits);
     for (int j = 1; j < J; ++j) pw[j] = sqr(pw[j - 1]);
+    if (trace) std::fprintf(stderr, "  to_decimal: %d powers %.3f s\n", J, tnow() - t0);
     std::vector<Nat> pieces{x};
     for (int j = J - 1; j >= 0; --j) {
+        const double tl = tnow();
         const Nat& D = pw[j];
         const size_t nd = bitlen(D), P = nd + 2 + 32;
         const Nat X = recip(D, P);
+        const double tr = tnow();
         const size_t m = pieces.size();
         std::vector<Nat> qs(m), rs(m);
         // quotient estimates of every piece in one batch
@@ -460,9 +470,14 @@ std::string to_decimal(const Nat& x, size_t width) {
             next[2 * i + 1] = std::move(rs[i]);
         }
         pieces.swap(next);
+        if (trace)
+            std::fprintf(stderr, "  to_decimal level %d: %zu pieces, reciprocal %.3f s, splits %.3f s\n", j, m, tr - tl,
+                         tnow() - tr);
     }
+    const double tleaf = tnow();
     std::string s(pieces.size() * kLeafDigits, '0');
     parallel_for(pieces.size(), [&](size_t i) { leaf_digits(pieces[i], &s[i * kLeafDigits]); });
+    if (trace) std::fprintf(stderr, "  to_decimal leaves: %.3f s\n", tnow() - tleaf);
     size_t first = s.find_first_not_of('0');
     if (first == std::string::npos) first = s.size() - 1;  // x == 0: "0"
     const size_t keep = std::max(width, s.size() - first);

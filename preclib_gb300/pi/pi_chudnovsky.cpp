@@ -24,6 +24,9 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#ifdef __GLIBC__
+#include <malloc.h>
+#endif
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -637,6 +640,13 @@ std::string short_form(const std::string& s, bool full) {
 }  // namespace
 
 int main(int argc, char** argv) {
+#ifdef __GLIBC__
+    // keep freed blocks of up to 32 MiB in the heap for reuse: the Newton
+    // steps and conversion levels allocate and free numbers of the same
+    // sizes over and over, and fresh pages cost a fault each
+    mallopt(M_MMAP_THRESHOLD, 32 << 20);
+    mallopt(M_TRIM_THRESHOLD, 1 << 30);
+#endif
     size_t digits = 100;
     bool phases = false, full = false;
     std::string file;

@@ -12,7 +12,7 @@
 // P(i)*C + c); a warp covers C columns x 32/C items, so every global access
 // moves whole 32-byte sectors.
 // Template parameters: SET prime set, M = log2 N1 (column length), C
-// columns per CTA, MR the pass radix cap (MR = 6: a 2^11-point column runs
+// columns per CTA (launched with 32*C threads), MR the pass radix cap (MR = 6: a 2^11-point column runs
 // as a radix-64 and a radix-32 pass; MR = 4: radix-8, -8, -32).  The
 // instantiated (SET, M, C, MR) configurations are PREC_COLS_CONFIGS; the
 // autotuner picks C and MR per transform length.

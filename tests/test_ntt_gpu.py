@@ -223,3 +223,53 @@ def test_launch_count(gpu):
     gpu.stream_check()
     b.close()
     assert gpu.launch_count() - c0 == 2 * (1 + 4)  # one single-CTA class, one four-step class
+
+
+def test_invalid_arguments(gpu):
+    """Null pointers with nonzero sizes and zero-size device operands are
+    refused with PREC_GPU_E_ARG; nothing is launched."""
+    import ctypes
+    L = gpu.lib()
+    a = O.splitmix64(1, 8)
+    out = np.zeros(16, np.uint64)
+    null = ctypes.POINTER(ctypes.c_uint64)()
+    c0 = gpu.launch_count()
+    assert L.prec_gpu_mul(null, 8, gpu._p(a), 8, gpu._p(out)) == gpu.E_ARG
+    assert L.prec_gpu_mul(gpu._p(a), 8, gpu._p(a), 8, null) == gpu.E_ARG
+    assert L.prec_gpu_sqr(null, 3, gpu._p(out)) == gpu.E_ARG
+    assert L.prec_gpu_mul_device(None, 5, 1, 5, 1, None) == gpu.E_ARG
+    assert L.prec_gpu_mul_device(1, 0, 1, 5, 1, None) == gpu.E_ARG
+    assert gpu.launch_count() == c0
+    # zero-length operands are a valid zero product
+    assert L.prec_gpu_mul(null, 0, gpu._p(a), 8, gpu._p(out)) == gpu.OK
+    assert not out[:8].any()
+
+
+def test_host_calls_from_many_threads(gpu):
+    """Host-pointer calls are serialised on one context: products from eight
+    threads at once, across both bands and squares, are all exact."""
+    import threading
+    shapes = [(20000, 15000), (3000, 2999), (200, 300), (65536, 65536), (9000, 9000), (1, 7), (6144, 6144),
+              (100000, 1000)]
+    cases = []
+    for i, (an, bn) in enumerate(shapes):
+        a = O.splitmix64(40 + i, an)
+        b = a if an == bn and i % 2 else O.splitmix64(50 + i, bn)
+        cases.append((a, b, O.mul_ntt(a, b)))
+    errors = []
+
+    def work(t):
+        try:
+            for r in range(3):
+                a, b, want = cases[(t + r) % len(cases)]
+                if not np.array_equal(gpu.mul(a, b), want):
+                    errors.append((t, r))
+        except Exception as e:  # pragma: no cover - reported below
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(8)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert not errors, errors

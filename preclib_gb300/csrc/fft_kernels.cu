@@ -65,36 +65,89 @@ __device__ __forceinline__ double bal_digit(const uint64_t* __restrict__ a, uint
     return (double)((int64_t)r - ((int64_t)t_out << b) + t_in);
 }
 
-// radix-2 stages over `narr` arrays of 2^m points in shared memory (array
-// stride `as` elements, element i at fpad(i)); sign -1 forward (DIF,
-// natural -> bit-reversed), +1 inverse (DIT, bit-reversed -> natural)
-template <bool DIT>
-__device__ void fft_stages(double2* s, int as, int narr, int m, const double2* __restrict__ tw) {
-    const int half_n = 1 << (m - 1);
-    for (int st = 0; st < m; ++st) {
-        const int bb = DIT ? st : m - 1 - st;  // paired index bit
-        const int h = 1 << bb;
-        for (int w = threadIdx.x; w < narr * half_n; w += blockDim.x) {
-            const int a = w / half_n, p = w % half_n;
-            const int j = p & (h - 1);
-            const int i0 = ((p >> bb) << (bb + 1)) | j;
-            double2* x = s + a * as + fpad(i0);
-            double2* y = s + a * as + fpad(i0 + h);
-            // w_{2h}^{+-j}
-            double2 r = root(tw, (uint32_t)j << (m - 1 - bb), m);
-            if (!DIT) r.y = -r.y;
-            const double2 xv = *x, yv = *y;
-            if (DIT) {
-                const double2 t = j ? cmul(yv, r) : yv;
-                *x = cadd(xv, t);
-                *y = csub(xv, t);
-            } else {
-                *x = cadd(xv, yv);
-                const double2 d = csub(xv, yv);
-                *y = j ? cmul(d, r) : d;
+// One register pass: stages over bits lo .. lo+RB-1 of `narr` arrays of 2^m
+// points in shared memory (array stride `as`, element i at fpad(i)); item u
+// holds elements base + (q << lo), q < 2^RB.  DIF (forward, sign -1,
+// natural -> bit-reversed) runs the pass's stages from its top bit down, DIT
+// (inverse, sign +1, bit-reversed -> natural) from its bottom bit up; the
+// stage at bit b pairs i and i + 2^b with twiddle w_(2^(b+1))^(i mod 2^b).
+template <bool DIT, int RB>
+__device__ __forceinline__ void fft_pass(double2* s, int as, int narr, int m, int lo, const double2* __restrict__ tw) {
+    const int lgper = m - RB;
+    const uint32_t lomask = (1u << lo) - 1;
+    for (int w = threadIdx.x; w < (narr << lgper); w += blockDim.x) {
+        const int a = w >> lgper;
+        const uint32_t u = w & ((1u << lgper) - 1);
+        const uint32_t base = ((u >> lo) << (lo + RB)) | (u & lomask);
+        const uint32_t ulo = u & lomask;
+        double2* row = s + a * as;
+        double2 x[1 << RB];
+#pragma unroll
+        for (int q = 0; q < (1 << RB); ++q) x[q] = row[fpad((int)(base + ((uint32_t)q << lo)))];
+#pragma unroll
+        for (int t = 0; t < RB; ++t) {
+            const int bb = DIT ? t : RB - 1 - t;
+            const int h = 1 << bb;
+#pragma unroll
+            for (int q = 0; q < (1 << RB); ++q) {
+                if (q & h) continue;
+                const uint32_t j = ulo | ((uint32_t)(q & (h - 1)) << lo);
+                const double2 X = x[q], Y = x[q + h];
+                double2 r = make_double2(1.0, 0.0);
+                if (j) {
+                    r = root(tw, j << (m - 1 - (lo + bb)), m);
+                    if (!DIT) r.y = -r.y;
+                }
+                if (DIT) {
+                    const double2 tt = j ? cmul(Y, r) : Y;
+                    x[q] = cadd(X, tt);
+                    x[q + h] = csub(X, tt);
+                } else {
+                    x[q] = cadd(X, Y);
+                    const double2 d = csub(X, Y);
+                    x[q + h] = j ? cmul(d, r) : d;
+                }
             }
         }
-        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < (1 << RB); ++q) row[fpad((int)(base + ((uint32_t)q << lo)))] = x[q];
+    }
+}
+
+template <bool DIT>
+__device__ __forceinline__ void fft_pass_rb(int rb, double2* s, int as, int narr, int m, int lo,
+                                            const double2* __restrict__ tw) {
+    if (rb == 3) fft_pass<DIT, 3>(s, as, narr, m, lo, tw);
+    else if (rb == 2) fft_pass<DIT, 2>(s, as, narr, m, lo, tw);
+    else fft_pass<DIT, 1>(s, as, narr, m, lo, tw);
+}
+
+// the whole 2^m-point transform of `narr` arrays in passes of up to radix
+// 2^PREC_FFT_MAX_RB, one barrier per pass; DIF from the top bits, DIT from the
+// bottom bits.  Radix 2 is the default: at 2^15 points radix-4 and radix-8
+// passes measured 10% and 30% slower (more registers per thread, the same
+// FP64 work, and these kernels are bound by the FP64 pipe and by latency).
+#ifndef PREC_FFT_MAX_RB
+#define PREC_FFT_MAX_RB 1
+#endif
+constexpr int kFftMaxRb = PREC_FFT_MAX_RB;
+
+template <bool DIT>
+__device__ void fft_stages(double2* s, int as, int narr, int m, const double2* __restrict__ tw) {
+    if (!DIT) {
+        for (int top = m; top > 0;) {
+            const int rb = top < kFftMaxRb ? top : kFftMaxRb;
+            fft_pass_rb<false>(rb, s, as, narr, m, top - rb, tw);
+            __syncthreads();
+            top -= rb;
+        }
+    } else {
+        for (int lo = 0; lo < m;) {
+            const int rb = m - lo < kFftMaxRb ? m - lo : kFftMaxRb;
+            fft_pass_rb<true>(rb, s, as, narr, m, lo, tw);
+            __syncthreads();
+            lo += rb;
+        }
     }
 }
 
@@ -108,6 +161,9 @@ __global__ void __launch_bounds__(256) k_fft_fwd_cols(FftArgs f) {
     const uint32_t N2 = 1u << f.k2;
     const int as = fpad(N1) + 1;
     const uint32_t c0 = blockIdx.x * C;
+    // the product's max distance starts at 0 (the previous product's readers
+    // are earlier in stream order)
+    if (blockIdx.x == 0 && threadIdx.x == 0) *f.maxdist = 0.0;
     for (int w = threadIdx.x; w < C * N1; w += blockDim.x) {
         const int col = w % C, i1 = w / C;
         const uint64_t i = (uint64_t)i1 * N2 + c0 + col;
@@ -188,6 +244,9 @@ __global__ void __launch_bounds__(256) k_fft_inv_cols(FftArgs f) {
         fsm[col * as + fpad(s)] = f.work[(uint64_t)s * N2 + c0 + col];
     }
     __syncthreads();
+    // block 0 alone reads the first element; the carry kernel's counter
+    // lives there and starts at 0
+    if (blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<unsigned long long*>(f.work) = 0ull;
     fft_stages<true>(fsm, as, C, f.k1, f.tw);
     const double inv_n = 1.0 / (double)(1u << f.k);
     double dmax = 0.0;
@@ -381,7 +440,10 @@ __global__ void k_fft_table(double2* tw) {
 
 // ---------------------------------------------------------------------------
 
-constexpr int kFftCols = 2;
+#ifndef PREC_FFT_COLS
+#define PREC_FFT_COLS 1
+#endif
+constexpr int kFftCols = PREC_FFT_COLS;  // columns per column-pass CTA
 
 size_t fft_table_bytes() { return (size_t)sizeof(double2) << (kFftMaxLog2 - 1); }
 
@@ -395,9 +457,9 @@ static size_t rows_smem(int k2) { return (size_t)2 * (fpad_host(1 << k2) + 1) * 
 
 int fft_configure_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_fft_fwd_cols<kFftCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)cols_smem(kFftMaxLog2 / 2));
+                                         (int)cols_smem(kFftMaxLog2 - kFftMaxLog2 / 2));
     if (!e) e = cudaFuncSetAttribute(k_fft_inv_cols<kFftCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)cols_smem(kFftMaxLog2 / 2));
+                                     (int)cols_smem(kFftMaxLog2 - kFftMaxLog2 / 2));
     if (!e) e = cudaFuncSetAttribute(k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)rows_smem(kFftMaxLog2 - kFftMaxLog2 / 2));
     return (int)e;
@@ -405,7 +467,6 @@ int fft_configure_kernels() {
 
 void fft_launch(const FftArgs& f, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], st);
-    cudaMemsetAsync(f.maxdist, 0, sizeof(double), st);
     const int ncol = (1 << f.k2) / kFftCols;
     k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
     if (ev) cudaEventRecord(ev[1], st);
@@ -417,7 +478,6 @@ void fft_launch(const FftArgs& f, cudaStream_t st, cudaEvent_t* ev) {
         const int64_t lcoef = (int64_t)(((uint64_t)f.b * f.ncoef + 63) / 64) + 2;
         const int64_t L = lcoef > (int64_t)f.lout ? lcoef : (int64_t)f.lout;
         const int nblk = (int)((L + kFftCarryBlockLimbs - 1) / kFftCarryBlockLimbs);
-        cudaMemsetAsync(f.work, 0, sizeof(uint64_t), st);  // the carry kernel's counter
         k_fft_carry<<<nblk, kFftCarryThreads, 0, st>>>(f);
     }
     count_launches(4);

@@ -457,7 +457,9 @@ static bool fft_plan_for(uint64_t la, uint64_t lb, FftPlan& fp) {
         if (!forced && fft_error_bound(b, k) >= 0.25) continue;
         fp.b = b;
         fp.k = k;
-        fp.k1 = k / 2;
+        // the longer half along the columns: twice the row-pair CTAs of the
+        // FP64-bound row kernel for odd k
+        fp.k1 = (k + 1) / 2;
         fp.k2 = k - fp.k1;
         fp.da = da;
         fp.db = db;

@@ -3,8 +3,10 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A step is one full product of two SplitMix64 operands (seeds 3 and 4) of
-1,048,576 uint64 limbs each (2,097,152-limb result, 2^22-point transforms
-over three primes).  Printed as ONE JSON line on rank 0:
+1,048,576 uint64 limbs each (2,097,152-limb result; by default 2^21-point
+transforms of whole 64-bit limbs over five primes, PREC_GPU_WIDE_DIGITS=0:
+2^22-point transforms of 32-bit digits over three).  Printed as ONE JSON
+line on rank 0:
   value  device time per product, operands already resident in HBM, L2
          flushed (256 MiB write) between timed steps; CUDA events on the
          stream the kernels run on
@@ -42,7 +44,7 @@ import numpy as np  # noqa: E402
 AN = BN = 1 << 20
 SEED_A, SEED_B = 3, 4
 METRIC = "1M×1M-limb mul ms"
-WORKLOAD = "1,048,576 x 1,048,576-limb uint64 product (SplitMix64 seeds 3,4), 2^22-point NTT x 3 primes"
+WORKLOAD = "1,048,576 x 1,048,576-limb uint64 product (SplitMix64 seeds 3,4)"
 GOLDEN = os.path.join(ROOT, "tests", "golden", "products.json")
 
 
@@ -294,6 +296,7 @@ def run_ours(args):
         native.check(L.prec_gpu_mul(native._p(pa), AN, native._p(pb), BN, native._p(po)))
         e2e.append(time.perf_counter() - t)
     e2e_exact = hashlib.sha256(np.ascontiguousarray(po, dtype="<u8").tobytes()).hexdigest() == golden
+    plan = native.last_stats()  # the plan of the product: transform length, primes, digit width
     e2e_ms = statistics.mean(e2e) * 1e3
     if dist:
         t = torch.tensor([e2e_ms], device=dev)
@@ -322,8 +325,10 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "an": AN, "bn": BN, "transform_points": n,
-                       "primes": 3, "l2": "flushed between timed steps (256 MiB write)",
+            "config": {"workload": WORKLOAD, "an": AN, "bn": BN,
+                       "transform_points": 1 << plan.log2_n, "primes": plan.primes,
+                       "digit_bits": plan.digit_bits, "canonical_points": n,
+                       "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "products_per_s": round(1e3 / per_product_ms, 2),
             "bit_exact": bool(bit_exact and e2e_exact),

@@ -44,6 +44,8 @@ enum {
 typedef struct prec_gpu_stats {
     int path;                 /* 0 single-CTA NTT, 1 four-step NTT, 2 FP64 FFT */
     int log2_n;               /* transform length */
+    int primes;               /* NTT primes (3, or 5 for 64-bit digits); 0 for the FFT */
+    int digit_bits;           /* bits per transform digit (NTT 32 or 64; FFT 8 .. 16) */
     size_t limbs_a, limbs_b;  /* operand sizes used */
     double fft_max_distance;  /* FP64 band: max |x - round(x)|; 0 for NTT */
     double device_ms;         /* device time of the product (events) */
@@ -254,6 +256,18 @@ int prec_gpu_last_stats(prec_gpu_stats_t *st);
 
 /* Transform length log2 the NTT band uses for an x bn limbs (0 if too large). */
 int prec_gpu_ntt_log2(size_t an, size_t bn);
+
+/* Digits of single NTT-band products (prec_gpu_mul, prec_gpu_sqr,
+ * prec_gpu_mul_ntt, prec_gpu_mul_device).  1 (the default; the environment
+ * variable PREC_GPU_WIDE_DIGITS=0 starts at 0): a product whose operands
+ * both fit in the lower half of a transform of at most 2^22 points takes
+ * whole 64-bit limbs as digits over five primes -- half the points of the
+ * 32-bit-digit transform -- when that needs fewer butterflies.  0: 32-bit
+ * digits over three primes.  The result is the same either way; the batch
+ * form and the serving loop always use 32-bit digits.  Returns the previous
+ * setting.  No counterpart in the reference, whose mul_ntt always splits
+ * limbs into 32-bit digits (src/mul_ntt.cpp:331-342). */
+int prec_gpu_set_wide_digits(int on);
 
 /* Static text for an error code. */
 const char *prec_gpu_strerror(int code);

@@ -1,7 +1,7 @@
 // ntt_cols.cuh -- column passes of the four-step NTT (index i = i1*N2 + i2).
 //
 // k_fwd_cols: for C adjacent columns i2 of one operand and one prime, the
-//   limbs are read as 32-bit digits (the reference's ntt_digits and mont_in,
+//   limbs are read as 32-bit digits (set 2: whole 64-bit limbs) (the reference's ntt_digits and mont_in,
 //   src/mul_ntt.cpp:331-342, 357-360, fused into the load), reduced, run
 //   through a DIF transform over i1 (the first log2(N1) stages of
 //   ntt_forward, mul_ntt.cpp:193-255) and multiplied by the four-step
@@ -26,6 +26,8 @@ namespace precgpu {
 // zero -- every operand of at most N/2 digits, i.e. both operands of a
 // balanced product: only the lower half is staged and reduced, and the
 // first stage (x, 0) -> (x, x*w) needs one twiddle product per pair.
+// Set 2 stages 64-bit limbs as two words per element (stage_limbs): the
+// element's digit is read from its row and the row 2^(M-1) above it.
 template <int SET, int M, int C, int MR>
 __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __restrict__ tw, const PrimeC& c) {
     using G = Geom<M, 0, MR>;
@@ -39,7 +41,9 @@ __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __
         uint32_t x[1][G::R];
 #pragma unroll
         for (int q = 0; q < H; ++q) {
-            const uint32_t d = Ar<SET>::digit(s[q * G::QS * C], c);
+            uint32_t d;
+            if constexpr (SET == kWideSet) d = Ar<SET>::digit64(s[q * G::QS * C], s[(q + H) * G::QS * C], c);
+            else d = Ar<SET>::digit(s[q * G::QS * C], c);
             const uint2 wq = __ldg(&tw[(1u << (G::LO + G::RB - 1)) + (ulo | ((uint32_t)q << G::LO))]);
             x[0][q] = d;
             x[0][q + H] = Ar<SET>::twiddle(d, wq, c);
@@ -72,19 +76,31 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
             P.scratch[i] = 0;
     }
 
-    const uint32_t* __restrict__ dig = reinterpret_cast<const uint32_t*>(operand ? P.b : P.a);
-    const uint64_t nd = 2 * (operand ? P.lb : P.la);
-    // the column tile of raw digits, staged by 16-byte asynchronous copies
-    // (digits past the operand read as zero), then the top pass reduces them
-    if (nd <= (1ull << (args.k - 1))) {
-        stage_rows<M, C>(sm, dig, N2, c0, nd, 0, 1 << (M - 1));
-        cp_async_wait<0>();
+    if constexpr (SET == kWideSet) {
+        // one digit per limb; the plan puts both operands in the lower half
+        const uint64_t nl = operand ? P.lb : P.la;
+        if (nl > (1ull << (args.k - 1))) {
+            if (threadIdx.x == 0) atomicOr(args.err, kDevErrPlan);
+            return;
+        }
+        stage_limbs<M, C>(sm, operand ? P.b : P.a, N2, c0, nl);
         __syncthreads();
         col_top_upper_zero<SET, M, C, MR>(sm, tw, pc);
     } else {
-        stage_cols<M, C>(sm, dig, N2, c0, nd);
-        __syncthreads();
-        col_pass<SET, M, 0, false, C, true, MR>(sm, tw, pc);
+        const uint32_t* __restrict__ dig = reinterpret_cast<const uint32_t*>(operand ? P.b : P.a);
+        const uint64_t nd = 2 * (operand ? P.lb : P.la);
+        // the column tile of raw digits, staged by 16-byte asynchronous copies
+        // (digits past the operand read as zero), then the top pass reduces them
+        if (nd <= (1ull << (args.k - 1))) {
+            stage_rows<M, C>(sm, dig, N2, c0, nd, 0, 1 << (M - 1));
+            cp_async_wait<0>();
+            __syncthreads();
+            col_top_upper_zero<SET, M, C, MR>(sm, tw, pc);
+        } else {
+            stage_cols<M, C>(sm, dig, N2, c0, nd);
+            __syncthreads();
+            col_pass<SET, M, 0, false, C, true, MR>(sm, tw, pc);
+        }
     }
     __syncthreads();
     col_passes<SET, M, 1, NP - 2, false, C, MR>(sm, tw, pc);
@@ -158,6 +174,13 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
     X(0, 9, 8, 6) X(0, 10, 4, 4) X(0, 10, 8, 4) X(0, 10, 4, 6) X(0, 10, 8, 6) X(0, 11, 4, 4)              \
     X(0, 11, 8, 4) X(0, 11, 4, 6) X(0, 11, 8, 6) X(1, 11, 4, 4) X(1, 11, 8, 4) X(1, 11, 4, 6)             \
     X(1, 11, 8, 6) X(1, 12, 4, 6) X(1, 13, 4, 6)
+
+// the forward column kernel of set 2 (64-bit digits) in the same (M, C, MR)
+// configurations as set 0; its other kernels are set 0's
+#define PREC_COLS_WIDE_CONFIGS(X)                                                                       \
+    X(2, 6, 4, 6) X(2, 6, 8, 6) X(2, 7, 4, 6) X(2, 7, 8, 6) X(2, 8, 4, 6) X(2, 8, 8, 6) X(2, 9, 4, 6)     \
+    X(2, 9, 8, 6) X(2, 10, 4, 4) X(2, 10, 8, 4) X(2, 10, 4, 6) X(2, 10, 8, 6) X(2, 11, 4, 4)              \
+    X(2, 11, 8, 4) X(2, 11, 4, 6) X(2, 11, 8, 6)
 
 inline size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
 

@@ -5,8 +5,9 @@
 namespace precgpu {
 
 void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
+    if (nprimes <= 0) nprimes = kSetPrimes[set];
     int cg, mr;
-    col_config(set, a.k1, a.cg, a.cmr, cg, mr);
+    col_config(set == kWideSet ? 0 : set, a.k1, a.cg, a.cmr, cg, mr);
     const dim3 grid((1u << a.k2) / cg, (a.square || a.operand_only ? 1 : 2) * nprimes, count);
     const size_t smem = col_smem(a.k1, cg);
 #define X(S, MM, CC, RR)                                                     \
@@ -16,6 +17,7 @@ void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
         return;                                                             \
     }
     PREC_COLS_CONFIGS(X)
+    PREC_COLS_WIDE_CONFIGS(X)
 #undef X
 }
 
@@ -25,6 +27,7 @@ int configure_fwd_cols() {
     if (!e) e = cudaFuncSetAttribute(k_fwd_cols<S, MM, CC, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)col_smem(MM, CC));
     PREC_COLS_CONFIGS(X)
+    PREC_COLS_WIDE_CONFIGS(X)
 #undef X
     return (int)e;
 }

@@ -244,6 +244,23 @@ __device__ __forceinline__ void stage_rows(uint32_t* sm, const uint32_t* __restr
     cp_async_commit();
 }
 
+// Whole 64-bit limbs (set 2) of an operand in the lower half of the tile:
+// rows i1 < 2^(M-1) of C columns; the low word of limb i1*ld + c0 + col
+// goes to row i1 and the high word to row i1 + 2^(M-1), the two elements
+// the top pass pairs anyway (limbs past `valid` read as zero).
+template <int M, int C>
+__device__ __forceinline__ void stage_limbs(uint32_t* sm, const uint64_t* __restrict__ g, uint64_t ld, uint64_t c0,
+                                            uint64_t valid) {
+    constexpr int H = 1 << (M - 1);
+    for (int w = threadIdx.x; w < H * C; w += blockDim.x) {
+        const int r = w / C, col = w % C;
+        const uint64_t idx = (uint64_t)r * ld + c0 + col;
+        const uint64_t v = idx < valid ? __ldg(&g[idx]) : 0ull;
+        sm[padded(r) * C + col] = (uint32_t)v;
+        sm[padded(r + H) * C + col] = (uint32_t)(v >> 32);
+    }
+}
+
 template <int M, int C>
 __device__ __forceinline__ void stage_cols(uint32_t* sm, const uint32_t* __restrict__ g, uint64_t ld, uint64_t c0,
                                            uint64_t valid) {

@@ -12,19 +12,28 @@ namespace precgpu {
 // Constants and device tables of one prime set, passed to every kernel by
 // value (kernel parameter space).
 struct FieldArgs {
-    PrimeC pc[kPrimes];
-    const uint2* tf[kPrimes];      // tf[(1<<b)+j] = (w_{2^{b+1}}^j, Shoup), b < 13
-    const uint2* ti[kPrimes];      // ti[(1<<b)+j] = (w_{2^{b+1}}^-j, Shoup)
-    const uint32_t* twhi[kPrimes]; // w_{2^L}^(h*2^13) * 2^32 mod p, L = set cap
-    const uint32_t* twlo[kPrimes]; // w_{2^L}^l * 2^32 mod p, l < 2^13
-    int max_log2;                  // L
-    int pad;
+    PrimeC pc[kMaxPrimes];
+    const uint2* tf[kMaxPrimes];      // tf[(1<<b)+j] = (w_{2^{b+1}}^j, Shoup), b < 13
+    const uint2* ti[kMaxPrimes];      // ti[(1<<b)+j] = (w_{2^{b+1}}^-j, Shoup)
+    const uint32_t* twhi[kMaxPrimes]; // w_{2^L}^(h*2^13) * 2^32 mod p, L = set cap
+    const uint32_t* twlo[kMaxPrimes]; // w_{2^L}^l * 2^32 mod p, l < 2^13
+    int max_log2;                     // L
+    int nprimes;                      // primes of the set
 };
 
 // CRT constants of one transform length (Garner with the transform's
 // scale 2^32 * N^-1 folded in; see crt3 in ntt_engine.cuh).
 struct CrtConst {
     ShoupC s1, k21, k22, k31, k32, k33;
+};
+
+// Garner constants of the five-prime set for one transform length:
+// v_j = y_j * a_j - sum_{i<j} v_i * b_{ij} (mod p_j), with
+// a_j = 2^32 N^-1 (p_1 .. p_{j-1})^-1 and b_{ij} = (p_i .. p_{j-1})^-1 mod p_j;
+// b_{ij} is b[j(j-1)/2 + i] (primes counted from 0).
+struct Crt5Const {
+    ShoupC a[5];
+    ShoupC b[10];
 };
 
 // One product of the multi-pass (four-step) path.
@@ -46,7 +55,8 @@ struct ProdArgs {
     int operand_only;   // forward columns of one operand: 1 = a, 2 = b (0: both)
     int rmr;            // row pass radix cap, 4 or 6 (0: default)
     int pad;
-    CrtConst crt;
+    CrtConst crt;       // sets 0 and 1
+    Crt5Const crt5;     // set 2
     FieldArgs f;
 };
 
@@ -100,6 +110,7 @@ struct SmallDesc {
 // device error bits
 constexpr int kDevErrTimeout = 1;
 constexpr int kDevErrCarry = 2;
+constexpr int kDevErrPlan = 4;  // a kernel was given a product its plan does not cover
 
 constexpr int kSmallMaxLog2 = 12;
 constexpr int kSmallMinLog2 = 5;
@@ -131,9 +142,9 @@ void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int cou
 // run as independent chains (fork from and join to the caller's stream), so
 // one prime's tail wave overlaps another prime's work.
 struct PrimeStreams {
-    cudaStream_t s[kPrimes];
+    cudaStream_t s[kMaxPrimes];
     cudaEvent_t fork;
-    cudaEvent_t join[kPrimes];
+    cudaEvent_t join[kMaxPrimes];
 };
 // With side streams, `a_ready` / `b_ready` (recorded on `st` after each
 // operand's upload) let each prime's forward columns of a start while b is
@@ -150,13 +161,15 @@ int ntt_row_threads(int k2, int n1, int* rows);
 int ntt_configure_kernels();  // opt-in shared-memory sizes; returns a cudaError_t
 
 // launchers of each translation unit (ntt_cols.cu, ntt_rows.cu, ntt_carry.cu, ntt_small.cu)
-// (primes a.prime0 .. a.prime0 + nprimes - 1)
+// (primes a.prime0 .. a.prime0 + nprimes - 1; 0 = every prime of the set).
+// The row and inverse column kernels of set 2 are set 0's: the same
+// arithmetic on residues, with set 2's primes and tables in a.f.
 void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
-                     int nprimes = kPrimes);
+                     int nprimes = 0);
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
-                 int nprimes = kPrimes);
+                 int nprimes = 0);
 void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
-                     int nprimes = kPrimes);
+                     int nprimes = 0);
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
                       int max_nblk = 0);
 int configure_fwd_cols();

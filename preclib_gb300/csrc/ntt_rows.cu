@@ -157,6 +157,8 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
 #define PREC_ROWS(X) PREC_ROWS1(X, false) PREC_ROWS1(X, true)
 
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
+    if (nprimes <= 0) nprimes = kSetPrimes[set];
+    if (set == kWideSet) set = 0;  // the same kernel on set 2's residues
     const int m = a.k2;
     const dim3 grid((1u << a.k1) / a.rows, nprimes, count);
     const int threads = a.rows << (m - 5);

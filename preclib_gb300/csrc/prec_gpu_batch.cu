@@ -170,7 +170,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
         const uint64_t need = 2 * (uint64_t)p.an + 2 * (uint64_t)p.bn - 1;
         int k = kSmallMinLog2;
         while ((1ull << k) < need) ++k;
-        if (k > kSetMaxLog2[kSets - 1]) {
+        if (k > kMaxLog2) {
             batch_free(b);
             return PREC_GPU_E_TOO_LARGE;
         }

@@ -30,10 +30,14 @@ typedef unsigned __int128 u128;
 
 // Prime sets (see ntt_field.cuh): set 0 for transforms up to 2^23 points,
 // set 1 -- the reference's primes and generators, src/mul_ntt.cpp:29-34 --
-// for 2^24 .. 2^26 points.
-static const uint32_t kP[kSets][kPrimes] = {{998244353u, 897581057u, 880803841u},
-                                            {469762049u, 1811939329u, 2013265921u}};
-static const uint32_t kG[kSets][kPrimes] = {{3u, 3u, 26u}, {3u, 13u, 31u}};
+// for 2^24 .. 2^26 points, set 2 (five primes, 64-bit digits) up to 2^22.
+static const uint32_t kP[kSets][kMaxPrimes] = {{998244353u, 897581057u, 880803841u},
+                                               {469762049u, 1811939329u, 2013265921u},
+                                               {998244353u, 985661441u, 943718401u, 935329793u, 918552577u}};
+static const uint32_t kG[kSets][kMaxPrimes] = {{3u, 3u, 26u}, {3u, 13u, 31u}, {3u, 3u, 7u, 3u, 5u}};
+// set 2 recovers every coefficient exactly while min(la, lb) stays below
+// p1..p5 / (2^64 - 1)^2 = 2344425.6
+constexpr uint64_t kWideMaxMinLimbs = 2344425;
 
 static uint32_t powmod(uint64_t b, uint64_t e, uint32_t m) {
     uint64_t r = 1 % m;
@@ -98,27 +102,62 @@ static CrtConst crt_compute(int set, int k) {
     return c;
 }
 
+// Garner constants of set 2 for 2^k points (Crt5Const): scale
+// s_j = 2^32 N^-1 (the Montgomery factor of the pointwise product and the
+// inverse transform's 1/N) folded into a_j.
+static Crt5Const crt5_compute(int k) {
+    const uint32_t* P = kP[kWideSet];
+    Crt5Const c;
+    for (int j = 0; j < 5; ++j) {
+        const uint32_t p = P[j];
+        const uint32_t R = (uint32_t)((1ull << 32) % p);
+        uint32_t a = mulmod(R, invmod((uint32_t)((1ull << k) % p), p), p);
+        for (int i = 0; i < j; ++i) a = mulmod(a, invmod(P[i] % p, p), p);
+        c.a[j] = shoup(a, p);
+        for (int i = 0; i < j; ++i) {
+            uint32_t b = 1;
+            for (int l = i; l < j; ++l) b = mulmod(b, invmod(P[l] % p, p), p);
+            c.b[j * (j - 1) / 2 + i] = shoup(b, p);
+        }
+    }
+    return c;
+}
+
 // CRT constants of every (set, length), computed once: plan_for runs once
 // per product of a batch, and a batch can hold millions of small products
 static CrtConst crt_for(int set, int k) {
-    constexpr int K = kSetMaxLog2[kSets - 1] + 1;
-    static CrtConst table[kSets][K];
+    static CrtConst table[2][kMaxLog2 + 1];
     static std::once_flag once;
     std::call_once(once, [] {
-        for (int s = 0; s < kSets; ++s)
+        for (int s = 0; s < 2; ++s)
             for (int j = kSmallMinLog2; j <= kSetMaxLog2[s]; ++j) table[s][j] = crt_compute(s, j);
     });
     return table[set][k];
 }
 
+static Crt5Const crt5_for(int k) {
+    static Crt5Const table[kMaxLog2 + 1];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (int j = kSmallMaxLog2 + 1; j <= kSetMaxLog2[kWideSet]; ++j) table[j] = crt5_compute(j);
+    });
+    return table[k];
+}
+
+static int ceil_log2(uint64_t n) {
+    int k = 0;
+    while ((1ull << k) < n) ++k;
+    return k;
+}
+
 // da, db: 32-bit digit counts (upper bounds are fine)
-int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
-    const uint64_t need = da + db - 1;
-    int k = kSmallMinLog2;
-    while ((1ull << k) < need) ++k;
-    if (k > kSetMaxLog2[kSets - 1]) return PREC_GPU_E_TOO_LARGE;
+int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
+    int k = ceil_log2(da + db - 1);
+    if (k < kSmallMinLog2) k = kSmallMinLog2;
+    if (k > kMaxLog2) return PREC_GPU_E_TOO_LARGE;
     pl.k = k;
     pl.set = k <= kSetMaxLog2[0] ? 0 : 1;
+    pl.nprimes = kPrimes;
     pl.crt = crt_for(pl.set, k);
     if (k <= kSmallMaxLog2) {
         pl.path = 0;
@@ -126,10 +165,27 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl) {
         return 0;
     }
     pl.path = 1;
+    if (wide) {
+        // 64-bit digits over five primes: half the points, both operands in
+        // the lower half of the transform (the forward column kernel's
+        // staging), taken when its butterflies (5 N' log N') undercut the
+        // 32-bit plan's (3 N log N)
+        const uint64_t la = (da + 1) / 2, lb = (db + 1) / 2;
+        const int kw = ceil_log2(la + lb - 1);
+        const uint64_t hi = la > lb ? la : lb, lo = la > lb ? lb : la;
+        if (kw > kSmallMaxLog2 && kw <= kSetMaxLog2[kWideSet] && 2 * hi <= (1ull << kw) && lo <= kWideMaxMinLimbs &&
+            5 * ((uint64_t)kw << kw) < 3 * ((uint64_t)k << k)) {
+            k = kw;
+            pl.k = k;
+            pl.set = kWideSet;
+            pl.nprimes = kMaxPrimes;
+            pl.crt5 = crt5_for(k);
+        }
+    }
     apply_config(pl, tuned_config(k));
     const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
     pl.nblk = (int)((lout + bl - 1) / bl);
-    pl.work_bytes = ((size_t)2 * kPrimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
+    pl.work_bytes = ((size_t)2 * pl.nprimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
     return 0;
 }
 
@@ -156,6 +212,21 @@ struct Ctx {
     cudaMemPool_t pool = nullptr;
     bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
 };
+
+// 64-bit digits (set 2) for single products: on unless PREC_GPU_WIDE_DIGITS=0;
+// prec_gpu_set_wide_digits changes it at run time
+static std::atomic<int> g_wide{-1};
+
+static bool wide_digits() {
+    int w = g_wide.load(std::memory_order_relaxed);
+    if (w < 0) {
+        const char* e = std::getenv("PREC_GPU_WIDE_DIGITS");
+        int expect = -1;
+        g_wide.compare_exchange_strong(expect, (e && e[0] == '0') ? 0 : 1);
+        w = g_wide.load(std::memory_order_relaxed);
+    }
+    return w != 0;
+}
 
 static Ctx g_ctx;
 
@@ -193,25 +264,27 @@ static int build_tables(Ctx& c) {
     const int T = 1 << kMaxSubLog2;   // entries of the Shoup tables
     const int H = 1 << kTwLevelBits;  // entries of each four-step level
     const size_t per_prime = (size_t)2 * T * sizeof(uint2) + (size_t)2 * H * sizeof(uint32_t);
-    std::vector<uint8_t> host(per_prime * kPrimes * kSets);
+    std::vector<uint8_t> host(per_prime * kMaxPrimes * kSets);
     CK(cudaMalloc(&c.tables, host.size()));
     for (int set = 0; set < kSets; ++set) {
         FieldArgs& fa = c.field[set];
         const int L = kSetMaxLog2[set];
         fa.max_log2 = L;
-        fa.pad = 0;
-        for (int j = 0; j < kPrimes; ++j) {
+        fa.nprimes = kSetPrimes[set];
+        for (int j = 0; j < kSetPrimes[set]; ++j) {
             const uint32_t p = kP[set][j];
             PrimeC& pc = fa.pc[j];
             pc.p = p;
             pc.pinv = neg_inv32(p);
             pc.one_wp = (uint32_t)((1ull << 32) / p);
             pc.p2 = 2 * p;
+            pc.r32 = (uint32_t)((1ull << 32) % p);
+            pc.r32p = shoup(pc.r32, p).wp;
             // g^((p-1)/2) == -1, so wL = g^((p-1)/2^L) has order exactly 2^L
             if (powmod(kG[set][j], (p - 1) / 2, p) != p - 1) return PREC_GPU_E_INTERNAL;
             if (((p - 1) >> L) << L != p - 1) return PREC_GPU_E_INTERNAL;
             const uint32_t wL = powmod(kG[set][j], (p - 1) >> L, p);
-            const size_t off = per_prime * (set * kPrimes + j);
+            const size_t off = per_prime * (set * kMaxPrimes + j);
             uint2* tf = reinterpret_cast<uint2*>(host.data() + off);
             uint2* ti = tf + T;
             uint32_t* twhi = reinterpret_cast<uint32_t*>(ti + T);
@@ -266,7 +339,7 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaEventCreateWithFlags(&c.ev_a, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c.ev_b, cudaEventDisableTiming));
     for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&c.stage_ev[i]));
-    for (int p = 0; p < kPrimes; ++p) {
+    for (int p = 0; p < kMaxPrimes; ++p) {
         CK(cudaStreamCreateWithFlags(&c.prime_streams.s[p], cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&c.prime_streams.join[p], cudaEventDisableTiming));
     }
@@ -374,7 +447,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.b = d_b;
         args.out = d_out;
         args.work = reinterpret_cast<uint32_t*>(c.ws);
-        args.scratch = args.work + ((size_t)2 * kPrimes << pl.k);
+        args.scratch = args.work + ((size_t)2 * pl.nprimes << pl.k);
         args.err = c.d_err;
         args.la = la;
         args.lb = lb;
@@ -389,6 +462,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.rmr = pl.rmr;
         args.square = square;
         args.crt = pl.crt;
+        args.crt5 = pl.crt5;
         args.f = c.field[pl.set];
         const bool split = c.split_primes && pl.split;
         ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready);
@@ -498,7 +572,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     const bool use_fft = ((mode == kModeBands && hi > kFftBandMin) || mode == kModeFft) && hi <= kFftBandMax &&
                          fft_plan_for(la, lb, fp);
     Plan pl;
-    if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl))) return r;
+    if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl, wide_digits()))) return r;
     if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
     // operands and result each start on a 256-byte boundary (32 limbs)
     const size_t la_pad = (la + 31) & ~(size_t)31, lb_pad = square ? 0 : (lb + 31) & ~(size_t)31;
@@ -552,6 +626,8 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     t_stats.path = use_fft ? 2 : pl.path;
     t_stats.log2_n = use_fft ? fp.k : pl.k;
+    t_stats.primes = use_fft ? 0 : pl.nprimes;
+    t_stats.digit_bits = use_fft ? fp.b : (pl.set == kWideSet ? 64 : 32);
     t_stats.device_ms = ms;
     t_stats.fft_max_distance = use_fft ? *c.h_maxdist : 0.0;
     if (fft_failed) return PREC_GPU_E_FFT_ROUNDING;
@@ -589,7 +665,7 @@ void prec_gpu_shutdown(void) {
     cudaEventDestroy(c.ev_a);
     cudaEventDestroy(c.ev_b);
     for (int i = 0; i <= kMaxStages; ++i) cudaEventDestroy(c.stage_ev[i]);
-    for (int p = 0; p < kPrimes; ++p) {
+    for (int p = 0; p < kMaxPrimes; ++p) {
         cudaStreamDestroy(c.prime_streams.s[p]);
         cudaEventDestroy(c.prime_streams.join[p]);
     }
@@ -634,7 +710,7 @@ int prec_gpu_mul_device(const uint64_t* d_a, size_t an, const uint64_t* d_b, siz
     if (r) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Plan pl;
-    if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl))) return r;
+    if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits()))) return r;
     if ((r = ensure_ws(c, pl.work_bytes))) return r;
     CK(cudaStreamWaitEvent(st, c.last_done, 0));
     if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st))) return r;
@@ -651,7 +727,7 @@ int prec_gpu_mul_device_profile(const uint64_t* d_a, size_t an, const uint64_t* 
     if (r) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Plan pl;
-    if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl))) return r;
+    if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits()))) return r;
     if ((r = ensure_ws(c, pl.work_bytes))) return r;
     CK(cudaStreamWaitEvent(st, c.last_done, 0));
     if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st, c.stage_ev))) return r;
@@ -691,10 +767,16 @@ int prec_gpu_last_stats(prec_gpu_stats_t* st) {
 
 uint64_t prec_gpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+int prec_gpu_set_wide_digits(int on) {
+    const int prev = wide_digits() ? 1 : 0;
+    g_wide.store(on ? 1 : 0, std::memory_order_relaxed);
+    return prev;
+}
+
 int prec_gpu_ntt_log2(size_t an, size_t bn) {
     if (an == 0 || bn == 0) return 0;
     Plan pl;
-    if (plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl)) return 0;
+    if (plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits())) return 0;
     return pl.k;
 }
 

@@ -23,14 +23,20 @@ struct Plan {
     int cmr = 0;   // column pass radix cap (0: default)
     int rmr = 0;   // row pass radix cap (0: default)
     int split = 0; // per-prime stream chains for a single product
-    CrtConst crt{};
+    int nprimes = 3;
+    CrtConst crt{};   // sets 0 and 1
+    Crt5Const crt5{}; // set 2
     size_t work_bytes = 0;  // work buffer + carry words of the four-step path
 };
 
 // da, db: 32-bit digit counts (upper bounds are fine); lout = La + Lb.
 // The four-step kernel configuration comes from the tuning table (the
 // autotuner's choice for the length, else the default configuration).
-int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl);
+// `wide`: the plan may take set 2 (whole 64-bit limbs as digits, five
+// primes, half the points) where that costs fewer butterflies; single
+// products do, the batch form, the serving loop and the autotuner keep
+// 32-bit digits.
+int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide = false);
 
 // Kernel configuration of one four-step transform length (the autotuner's
 // unit; prec_gpu_tune.cu).

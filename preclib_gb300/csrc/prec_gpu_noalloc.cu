@@ -160,7 +160,7 @@ static int noalloc_setup(int dev, cudaStream_t stream, NoAllocDevice*& out) {
         if (e != cudaSuccess) return na_code(e);
         FieldArgs& f = d.field;
         f.max_log2 = kNaL;
-        f.pad = 0;
+        f.nprimes = kPrimes;
         for (int j = 0; j < kPrimes; ++j) {
             const uint32_t p = kNaP[j];
             uint32_t inv = 1;

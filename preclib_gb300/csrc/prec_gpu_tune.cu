@@ -28,7 +28,7 @@ namespace precgpu {
 namespace {
 
 constexpr int kTuneMin = kSmallMaxLog2 + 1;         // first four-step length
-constexpr int kTuneMax = kSetMaxLog2[kSets - 1];   // 26
+constexpr int kTuneMax = kMaxLog2;                 // 26
 constexpr int kSplitMinLog2 = 19;  // default: per-prime streams from 2^19 points
 
 struct Entry {

@@ -27,15 +27,15 @@ EXPORTS = (
     "prec_gpu_batch_destroy", "prec_gpu_mul_batch", "prec_gpu_serve_create", "prec_gpu_serve_submit",
     "prec_gpu_serve_wait", "prec_gpu_serve_drain", "prec_gpu_serve_stats", "prec_gpu_serve_destroy",
     "prec_gpu_sqr", "prec_gpu_autotune", "prec_gpu_tune_get", "prec_gpu_tune_set", "prec_gpu_tune_reset",
-    "prec_gpu_tune_save", "prec_gpu_tune_load", "prec_gpu_launch_count",
+    "prec_gpu_tune_save", "prec_gpu_tune_load", "prec_gpu_launch_count", "prec_gpu_set_wide_digits",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 
 
 class Stats(ctypes.Structure):
-    _fields_ = [("path", ctypes.c_int), ("log2_n", ctypes.c_int),
-                ("limbs_a", ctypes.c_size_t), ("limbs_b", ctypes.c_size_t),
+    _fields_ = [("path", ctypes.c_int), ("log2_n", ctypes.c_int), ("primes", ctypes.c_int),
+                ("digit_bits", ctypes.c_int), ("limbs_a", ctypes.c_size_t), ("limbs_b", ctypes.c_size_t),
                 ("fft_max_distance", ctypes.c_double), ("device_ms", ctypes.c_double)]
 
 
@@ -91,6 +91,8 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_sqr.restype = ctypes.c_int
         L.prec_gpu_launch_count.argtypes = []
         L.prec_gpu_launch_count.restype = ctypes.c_uint64
+        L.prec_gpu_set_wide_digits.argtypes = [ctypes.c_int]
+        L.prec_gpu_set_wide_digits.restype = ctypes.c_int
         L.prec_gpu_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneEntry), ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t)]
         L.prec_gpu_autotune.restype = ctypes.c_int
@@ -212,6 +214,12 @@ def autotune(kmin: int = 13, kmax: int = 26):
 def launch_count() -> int:
     """Kernel launches the library has issued in this process."""
     return int(lib().prec_gpu_launch_count())
+
+
+def set_wide_digits(on: bool) -> bool:
+    """64-bit digits over five primes for single NTT-band products (True, the
+    default) or 32-bit digits over three primes; returns the previous setting."""
+    return bool(lib().prec_gpu_set_wide_digits(1 if on else 0))
 
 
 def tune_get(log2_n: int) -> dict:

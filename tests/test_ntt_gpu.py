@@ -36,23 +36,34 @@ def test_kat_square(gpu):
                                    (2047, 2049), (2048, 2048), (2049, 2049), (4096, 4095),
                                    (4097, 4097), (6144, 8192), (8192, 8192), (10000, 5001),
                                    (16384, 16384), (40000, 39999), (65536, 65536), (100001, 50001)])
-def test_random_vs_oracle(gpu, an, bn):
+@pytest.mark.parametrize("wide", [False, True])
+def test_random_vs_oracle(gpu, an, bn, wide):
     a = O.splitmix64(an * 31 + bn, an)
     b = O.splitmix64(an * 37 + bn + 1, bn)
-    got = gpu.mul(a, b, ntt=True)
+    prev = gpu.set_wide_digits(wide)
+    try:
+        got = gpu.mul(a, b, ntt=True)
+    finally:
+        gpu.set_wide_digits(prev)
     assert np.array_equal(got, O.mul_ntt(a, b))
 
 
-def test_both_paths_each_length(gpu):
-    """Every transform length 2^5 .. 2^19 (single-CTA and four-step)."""
-    for k in range(5, 20):
-        n = 1 << (k - 2)  # 2n digits per operand -> N = 2^k
-        a = O.splitmix64(k, n)
-        b = O.splitmix64(k + 100, n)
-        a[-1] |= np.uint64(1 << 63)
-        b[-1] |= np.uint64(1 << 63)
-        got = gpu.mul(a, b, ntt=True)
-        assert np.array_equal(got, O.mul_ntt(a, b)), k
+@pytest.mark.parametrize("wide", [False, True])
+def test_both_paths_each_length(gpu, wide):
+    """Every transform length 2^5 .. 2^19 (single-CTA and four-step), with
+    32-bit digits and with 64-bit digits where the plan takes them."""
+    prev = gpu.set_wide_digits(wide)
+    try:
+        for k in range(5, 20):
+            n = 1 << (k - 2)  # 2n digits per operand -> N = 2^k
+            a = O.splitmix64(k, n)
+            b = O.splitmix64(k + 100, n)
+            a[-1] |= np.uint64(1 << 63)
+            b[-1] |= np.uint64(1 << 63)
+            got = gpu.mul(a, b, ntt=True)
+            assert np.array_equal(got, O.mul_ntt(a, b)), k
+    finally:
+        gpu.set_wide_digits(prev)
 
 
 def test_zero_and_padding(gpu):
@@ -121,11 +132,18 @@ def test_large_mod_prime_spot_checks(gpu):
 
 
 def test_1m_golden(gpu, golden):
+    """The 1M x 1M product on both digit widths: 2^21 points over five primes
+    (64-bit digits, the default) and 2^22 points over three (32-bit)."""
     rec = [r for r in golden if r["name"] == "cfg2_1Mx1M_ntt"][0]
     a, b = patterns.make(rec["gen"])
-    assert _digest(gpu.mul(a, b, ntt=True)) == rec["sha256"]
-    st = gpu.last_stats()
-    assert st.log2_n == 22 and st.path == 1
+    for wide, k in ((True, 21), (False, 22)):
+        prev = gpu.set_wide_digits(wide)
+        try:
+            assert _digest(gpu.mul(a, b, ntt=True)) == rec["sha256"], wide
+            st = gpu.last_stats()
+            assert st.log2_n == k and st.path == 1
+        finally:
+            gpu.set_wide_digits(prev)
 
 
 def test_device_api_matches_host_api(gpu):
@@ -199,17 +217,23 @@ def test_host_api_pinned_result_buffer(gpu):
 
 
 def test_launch_count(gpu):
-    """prec_gpu_launch_count: 10 kernels for a 2^22-point product (three per
-    prime on side streams, then the CRT), 1 for a single-CTA product, and a
-    batch graph's kernels at every replay."""
+    """prec_gpu_launch_count: three kernels per prime on side streams, then
+    the CRT -- 16 for a 1M-limb product on 64-bit digits (five primes), 10
+    on 32-bit digits (three) -- 1 for a single-CTA product, and a batch
+    graph's kernels at every replay."""
     torch = pytest.importorskip("torch")
     n = 1 << 20
     ta = torch.from_numpy(O.splitmix64(1, n).view(np.int64)).cuda()
     to = torch.empty(2 * n, dtype=torch.int64, device="cuda")
-    c0 = gpu.launch_count()
-    gpu.mul_device(ta.data_ptr(), n, ta.data_ptr() + 8 * 7, n - 7, to.data_ptr())
-    gpu.stream_check()
-    assert gpu.launch_count() - c0 == 10
+    for wide, launches in ((True, 16), (False, 10)):
+        prev = gpu.set_wide_digits(wide)
+        try:
+            c0 = gpu.launch_count()
+            gpu.mul_device(ta.data_ptr(), n, ta.data_ptr() + 8 * 7, n - 7, to.data_ptr())
+            gpu.stream_check()
+            assert gpu.launch_count() - c0 == launches, wide
+        finally:
+            gpu.set_wide_digits(prev)
     c0 = gpu.launch_count()
     gpu.mul_device(ta.data_ptr(), 100, ta.data_ptr() + 800, 90, to.data_ptr())
     gpu.stream_check()

@@ -40,18 +40,27 @@ def test_sqr_vs_oracle(gpu, n):
 
 def test_sqr_each_length(gpu):
     """Every transform length 2^5 .. 2^21, both the single-CTA and the
-    four-step kernels, squares of operands with the top bit set."""
-    for k in range(5, 22):
-        n = 1 << (k - 2)
-        a = O.splitmix64(k + 500, n)
-        a[-1] |= np.uint64(1 << 63)
-        assert np.array_equal(gpu.mul(a, a, ntt=True), O.mul_ntt(a, a)), k
-        assert gpu.last_stats().log2_n == k
+    four-step kernels, squares of operands with the top bit set: 32-bit
+    digits (2^k points for 2^(k-2) limbs), then 64-bit digits (2^(k-1)
+    points from 2^13)."""
+    for wide in (False, True):
+        prev = gpu.set_wide_digits(wide)
+        try:
+            for k in range(5, 22):
+                n = 1 << (k - 2)
+                a = O.splitmix64(k + 500, n)
+                a[-1] |= np.uint64(1 << 63)
+                assert np.array_equal(gpu.mul(a, a, ntt=True), O.mul_ntt(a, a)), (wide, k)
+                assert gpu.last_stats().log2_n == (k - 1 if wide and k >= 14 else k)
+        finally:
+            gpu.set_wide_digits(prev)
 
 
 def test_sqr_all_ones(gpu):
-    """(2^(64n) - 1)^2 = 2^(128n) - 2^(64n+1) + 1: maximal carries."""
-    for n in (5000, 70000, 1 << 20):
+    """(2^(64n) - 1)^2 = 2^(128n) - 2^(64n+1) + 1: maximal carries; at
+    n = 2^21 the largest coefficient, n (2^64 - 1)^2, is within 2^0.16 of the
+    five primes' product."""
+    for n in (5000, 70000, 1 << 20, 1 << 21):
         a = np.full(n, np.uint64(0xFFFFFFFFFFFFFFFF))
         got = gpu.sqr(a)
         want = np.zeros(2 * n, np.uint64)
@@ -68,13 +77,19 @@ def _spot(p, a):
 
 
 def test_sqr_large_both_prime_sets(gpu):
-    """2^22-point (prime set 0) and 2^24 / 2^25-point (prime set 1) squares."""
-    for (n, s, k) in ((1 << 20, 3, 22), (3 << 20, 4, 24), (3 << 21, 5, 25)):
-        a = O.splitmix64(s, n)
-        p = gpu.sqr(a)
-        assert gpu.last_stats().log2_n == k
-        _spot(p, a)
-        assert p[-1] != 0
+    """2^22-point (prime set 0, 32-bit digits), 2^21- and 2^22-point (set 2,
+    64-bit digits) and 2^24 / 2^25-point (prime set 1) squares."""
+    for (n, s, k, wide) in ((1 << 20, 3, 22, False), (1 << 20, 3, 21, True), (1 << 21, 6, 22, True),
+                            (3 << 20, 4, 24, True), (3 << 21, 5, 25, True)):
+        prev = gpu.set_wide_digits(wide)
+        try:
+            a = O.splitmix64(s, n)
+            p = gpu.sqr(a)
+            assert gpu.last_stats().log2_n == k
+            _spot(p, a)
+            assert p[-1] != 0
+        finally:
+            gpu.set_wide_digits(prev)
 
 
 def test_sqr_device_same_pointer(gpu):

@@ -33,10 +33,16 @@ def _configs(gpu, k):
     return out
 
 
+@pytest.mark.parametrize("wide", [False, True])
 @pytest.mark.parametrize("k", [13, 16, 20, 22])
-def test_every_config_bit_exact(gpu, k):
+def test_every_config_bit_exact(gpu, k, wide):
+    """Every kernel configuration of a length, on 32-bit digits and on 64-bit
+    digits (the same kernels on five primes' residues)."""
     n = 1 << (k - 2)
-    shapes = [(n, n), (n + n // 2 - 3, n // 2 + 1)]  # balanced, and one operand above N/2 digits
+    if wide:  # both operands within the lower half of 2^k points of 64-bit digits
+        shapes = [(2 * n, 2 * n), (2 * n, n + 1)]
+    else:  # balanced, and one operand above N/2 digits
+        shapes = [(n, n), (n + n // 2 - 3, n // 2 + 1)]
     cases = []
     for an, bn in shapes:
         a = O.splitmix64(k * 7 + an, an)
@@ -44,12 +50,17 @@ def test_every_config_bit_exact(gpu, k):
         cases.append((a, b, O.mul_ntt(a, b)))
     cfgs = _configs(gpu, k)
     assert len(cfgs) >= 8
-    for cfg in cfgs:
-        gpu.tune_set(**cfg)
-        for a, b, want in cases:
-            got = gpu.mul(a, b, ntt=True)
-            assert gpu.last_stats().log2_n == k
-            assert np.array_equal(got, want), cfg
+    prev = gpu.set_wide_digits(wide)
+    try:
+        for cfg in cfgs:
+            gpu.tune_set(**cfg)
+            for a, b, want in cases:
+                got = gpu.mul(a, b, ntt=True)
+                assert gpu.last_stats().log2_n == k
+                assert np.array_equal(got, want), cfg
+    finally:
+        gpu.set_wide_digits(prev)
+        gpu.tune_reset()
 
 
 def _spot(p, a, b):

@@ -128,6 +128,7 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
             args.rmr = c.pl.rmr;
             args.square = c.square;
             args.crt = c.pl.crt;
+            args.crt5 = c.pl.crt5;
             args.f = ctx_field(c.pl.set);
             for (const Chunk& ch : c.chunks)
                 ntt_launch_4step_batch(c.pl.set, args, c.d_ptrs + ch.first, ch.count, ch.max_nblk, st);
@@ -154,7 +155,8 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
     b->oneshot = ost;
     b->items.assign(items, items + count);
     b->err = ctx_device_err();
-    std::map<int, Cls> by_k;  // key 2k + square
+    std::map<int, Cls> by_k;  // key: 64-bit digits << 8 | k << 1 | square
+    const bool wide = wide_digits();
     for (size_t i = 0; i < count; ++i) {
         const prec_gpu_product_t& p = items[i];
         if ((p.an && !p.a) || (p.bn && !p.b) || (p.an + p.bn && !p.out)) {
@@ -165,8 +167,9 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             b->zero_items.push_back((int)i);
             continue;
         }
-        // the transform length alone picks the class; the class plan (CRT
-        // constants, kernel configuration) is made once, for its first product
+        // the transform length and digit width pick the class; the class
+        // plan (CRT constants, kernel configuration) is made once, for its
+        // first product
         const uint64_t need = 2 * (uint64_t)p.an + 2 * (uint64_t)p.bn - 1;
         int k = kSmallMinLog2;
         while ((1ull << k) < need) ++k;
@@ -174,12 +177,18 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             batch_free(b);
             return PREC_GPU_E_TOO_LARGE;
         }
+        const int kw = wide ? wide_log2(p.an, p.bn, k) : 0;
+        if (kw) k = kw;
         const int sq = (p.a == p.b && p.an == p.bn && k > kSmallMaxLog2) ? 1 : 0;
-        Cls& c = by_k[2 * k + sq];
+        Cls& c = by_k[(kw ? 1 << 8 : 0) | k << 1 | sq];
         if (c.items.empty()) {
-            if ((r = plan_for(2 * (uint64_t)p.an, 2 * (uint64_t)p.bn, p.an + p.bn, c.pl))) {
+            if ((r = plan_for(2 * (uint64_t)p.an, 2 * (uint64_t)p.bn, p.an + p.bn, c.pl, wide))) {
                 batch_free(b);
                 return r;
+            }
+            if (c.pl.k != k || (c.pl.set == kWideSet) != (kw != 0)) {  // the key and the plan agree
+                batch_free(b);
+                return PREC_GPU_E_INTERNAL;
             }
             c.k = c.pl.k;
             c.square = sq;
@@ -196,8 +205,11 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
         desc_off.push_back(bytes);
         bytes += align256(n * (c.pl.path == 0 ? sizeof(SmallDesc) : sizeof(ProdPtrs)));
         if (c.pl.path == 1) {
-            const size_t carry_words = (size_t)(((1ull << c.k) / 2) / (kCarryThreads * kCarryLimbs)) + 2;
-            c.ws_per = align256(((size_t)2 * kPrimes << c.k) * sizeof(uint32_t) + carry_words * sizeof(uint32_t));
+            // a product of 2^k points has at most 2^(k-1) + 1 limbs on 32-bit
+            // digits, 2^k + 1 on 64-bit digits
+            const uint64_t lout_max = c.pl.set == kWideSet ? (1ull << c.k) + 1 : (1ull << c.k) / 2 + 1;
+            const size_t carry_words = (size_t)(lout_max / (kCarryThreads * kCarryLimbs)) + 2;
+            c.ws_per = align256(((size_t)2 * c.pl.nprimes << c.k) * sizeof(uint32_t) + carry_words * sizeof(uint32_t));
             c.per_chunk = (int)std::min<size_t>({n, std::max<size_t>(1, budget / c.ws_per), 65535});
             ws_off.push_back(bytes);
             bytes += c.ws_per * c.per_chunk;
@@ -250,7 +262,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
                 d.b = p.b;
                 d.out = p.out;
                 d.work = reinterpret_cast<uint32_t*>(w);
-                d.scratch = d.work + ((size_t)2 * kPrimes << c.k);
+                d.scratch = d.work + ((size_t)2 * c.pl.nprimes << c.k);
                 d.la = p.an;
                 d.lb = p.bn;
                 d.lout = p.an + p.bn;

@@ -150,6 +150,16 @@ static int ceil_log2(uint64_t n) {
     return k;
 }
 
+int wide_log2(uint64_t la, uint64_t lb, int k32) {
+    if (k32 <= kSmallMaxLog2) return 0;
+    const int kw = ceil_log2(la + lb - 1);
+    const uint64_t hi = la > lb ? la : lb, lo = la > lb ? lb : la;
+    if (kw > kSmallMaxLog2 && kw <= kSetMaxLog2[kWideSet] && 2 * hi <= (1ull << kw) && lo <= kWideMaxMinLimbs &&
+        5 * ((uint64_t)kw << kw) < 3 * ((uint64_t)k32 << k32))
+        return kw;
+    return 0;
+}
+
 // da, db: 32-bit digit counts (upper bounds are fine)
 int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
     int k = ceil_log2(da + db - 1);
@@ -166,15 +176,8 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
     }
     pl.path = 1;
     if (wide) {
-        // 64-bit digits over five primes: half the points, both operands in
-        // the lower half of the transform (the forward column kernel's
-        // staging), taken when its butterflies (5 N' log N') undercut the
-        // 32-bit plan's (3 N log N)
-        const uint64_t la = (da + 1) / 2, lb = (db + 1) / 2;
-        const int kw = ceil_log2(la + lb - 1);
-        const uint64_t hi = la > lb ? la : lb, lo = la > lb ? lb : la;
-        if (kw > kSmallMaxLog2 && kw <= kSetMaxLog2[kWideSet] && 2 * hi <= (1ull << kw) && lo <= kWideMaxMinLimbs &&
-            5 * ((uint64_t)kw << kw) < 3 * ((uint64_t)k << k)) {
+        const int kw = wide_log2((da + 1) / 2, (db + 1) / 2, k);
+        if (kw) {
             k = kw;
             pl.k = k;
             pl.set = kWideSet;
@@ -217,7 +220,7 @@ struct Ctx {
 // prec_gpu_set_wide_digits changes it at run time
 static std::atomic<int> g_wide{-1};
 
-static bool wide_digits() {
+bool wide_digits() {
     int w = g_wide.load(std::memory_order_relaxed);
     if (w < 0) {
         const char* e = std::getenv("PREC_GPU_WIDE_DIGITS");

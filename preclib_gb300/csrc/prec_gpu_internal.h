@@ -34,9 +34,16 @@ struct Plan {
 // autotuner's choice for the length, else the default configuration).
 // `wide`: the plan may take set 2 (whole 64-bit limbs as digits, five
 // primes, half the points) where that costs fewer butterflies; single
-// products do, the batch form, the serving loop and the autotuner keep
-// 32-bit digits.
+// products, the batch form and the serving loop pass wide_digits(), the
+// autotuner keeps 32-bit digits.
 int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide = false);
+// log2 of the 64-bit-digit (set 2) transform for la x lb limbs, or 0 where
+// the 32-bit plan of 2^k32 points stays: set 2 needs 2^13 .. 2^22 points,
+// both operands in the lower half, min(la, lb) within the five primes'
+// bound, and fewer butterflies (5 N' log N' < 3 N log N)
+int wide_log2(uint64_t la, uint64_t lb, int k32);
+// 64-bit digits allowed (prec_gpu_set_wide_digits; PREC_GPU_WIDE_DIGITS)
+bool wide_digits();
 
 // Kernel configuration of one four-step transform length (the autotuner's
 // unit; prec_gpu_tune.cu).

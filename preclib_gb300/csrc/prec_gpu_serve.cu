@@ -107,7 +107,7 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         args.b = p.b;
         args.out = p.out;
         args.work = static_cast<uint32_t*>(ws);
-        args.scratch = args.work + ((size_t)2 * kPrimes << r.pl.k);
+        args.scratch = args.work + ((size_t)2 * r.pl.nprimes << r.pl.k);
         args.err = s->err;
         args.la = p.an;
         args.lb = p.bn;
@@ -121,6 +121,7 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         args.cmr = r.pl.cmr;
         args.rmr = r.pl.rmr;
         args.crt = r.pl.crt;
+        args.crt5 = r.pl.crt5;
         args.f = ctx_field(r.pl.set);
         ntt_launch_4step(r.pl.set, args, st);
         cudaFreeAsync(ws, st);
@@ -248,7 +249,7 @@ int prec_gpu_serve_submit(prec_gpu_server_t* s, const uint64_t* d_a, size_t an, 
     Request r;
     r.p = prec_gpu_product_t{d_a, an, d_b, bn, d_out};
     if (an && bn) {
-        const int rc = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, r.pl);
+        const int rc = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, r.pl, wide_digits());
         if (rc) return rc;
         r.bytes = footprint(r.pl);
         if (r.bytes > s->budget) return PREC_GPU_E_NOMEM;  // could never be admitted

@@ -131,3 +131,29 @@ def test_config3_workload_tuned_vs_oracle(gpu):
             assert np.array_equal(out[o:o + a_ + b_], _plain(gpu, torch, db, i)), sizes[i]
     finally:
         gpu.tune_reset()
+
+
+def test_batch_both_digit_widths(gpu):
+    """The same batch planned with 64-bit digits allowed (classes of five
+    primes where the shapes fit) and with 32-bit digits only: identical
+    limbs, and a sample equals the oracle."""
+    torch = pytest.importorskip("torch")
+    sizes = _sizes(13, 150, lo_max=200000)
+    db = DevBatch(torch, sizes, 31)
+    outs = []
+    for wide in (False, True):
+        prev = gpu.set_wide_digits(wide)
+        try:
+            db.out.fill_(-1)
+            b = gpu.Batch(db.items())
+            b.run()
+            gpu.stream_check()
+            b.close()
+            outs.append(db.out.cpu().numpy().copy())
+        finally:
+            gpu.set_wide_digits(prev)
+    assert np.array_equal(outs[0], outs[1])
+    for i in range(0, len(sizes), 13):
+        a, b = db.operands(i)
+        if len(a) and len(b):
+            assert np.array_equal(db.result(i), O.mul_ntt(a, b)), sizes[i]

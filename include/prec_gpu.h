@@ -31,7 +31,7 @@ extern "C" {
 enum {
     PREC_GPU_OK = 0,
     PREC_GPU_E_ARG = 1,          /* null pointer, zero or inconsistent size */
-    PREC_GPU_E_TOO_LARGE = 2,    /* product beyond the 2^26-point transform */
+    PREC_GPU_E_TOO_LARGE = 2,    /* product beyond the 2^26-point transform (batch and serving forms) */
     PREC_GPU_E_NOMEM = 3,        /* device allocation failed */
     PREC_GPU_E_CUDA = 4,         /* other CUDA runtime error */
     PREC_GPU_E_TIMEOUT = 5,      /* a bounded device-side wait ran out */
@@ -42,7 +42,7 @@ enum {
 
 /* Per-product report of the most recent call on the calling thread. */
 typedef struct prec_gpu_stats {
-    int path;                 /* 0 single-CTA NTT, 1 four-step NTT, 2 FP64 FFT */
+    int path;                 /* 0 single-CTA NTT, 1 four-step NTT, 2 FP64 FFT, 3 blocked NTT */
     int log2_n;               /* transform length */
     int primes;               /* NTT primes (3, or 5 for 64-bit digits); 0 for the FFT */
     int digit_bits;           /* bits per transform digit (NTT 32 or 64; FFT 8 .. 16) */
@@ -143,7 +143,9 @@ int prec_gpu_fft_digit_bits(size_t an, size_t bn);
  * stay as given (no trimming of zero high limbs).  The call returns after
  * enqueueing; device-side failures (bounded waits) are reported by
  * prec_gpu_stream_check.  Successive calls share the library's workspace
- * and are ordered after one another even across streams. */
+ * and are ordered after one another even across streams.  d_out must not
+ * overlap the operands.  Operands above the block size run blocked (see
+ * prec_gpu_set_block_limbs). */
 int prec_gpu_mul_device(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
                         uint64_t *d_out, void *stream);
 
@@ -254,7 +256,8 @@ int prec_gpu_stream_check(void *stream);
 /* Report of the last completed host-pointer call on this thread. */
 int prec_gpu_last_stats(prec_gpu_stats_t *st);
 
-/* Transform length log2 the NTT band uses for an x bn limbs (0 if too large). */
+/* Transform length log2 the NTT band uses for an x bn limbs; 0 when the
+ * product runs blocked (an operand above the block size). */
 int prec_gpu_ntt_log2(size_t an, size_t bn);
 
 /* Digits of single NTT-band products (prec_gpu_mul, prec_gpu_sqr,
@@ -268,6 +271,16 @@ int prec_gpu_ntt_log2(size_t an, size_t bn);
  * setting.  No counterpart in the reference, whose mul_ntt always splits
  * limbs into 32-bit digits (src/mul_ntt.cpp:331-342). */
 int prec_gpu_set_wide_digits(int on);
+
+/* Block size of blocked products, in limbs (default and maximum 2^24 =
+ * 16,777,216; at least 1024; 0 restores the default).  A product through
+ * prec_gpu_mul, prec_gpu_sqr, prec_gpu_mul_ntt or prec_gpu_mul_device
+ * whose larger operand exceeds it is cut into blocks of at most this many
+ * limbs: every pair of blocks is one NTT-band product, added into the
+ * result at its offset on the device.  Replaces: the reference's mul_ntt
+ * guard that hands operands above 2^24 limbs to mul_fft
+ * (src/mul_ntt.cpp:494-518).  Returns the previous setting. */
+size_t prec_gpu_set_block_limbs(size_t limbs);
 
 /* Static text for an error code. */
 const char *prec_gpu_strerror(int code);

@@ -196,4 +196,11 @@ inline void col_config(int set, int m, int req_cg, int req_mr, int& cg, int& mr)
 int configure_rows();
 int configure_small();
 
+// out[0 .. n) += t[0 .. nt) (nt <= n), the carry running on into out's
+// higher limbs (ntt_add.cu); scratch holds add_into_scratch_words(nt)
+// words; a carry past out[n - 1] sets kDevErrCarry in *err
+size_t add_into_scratch_words(uint64_t nt);
+void launch_add_into(uint64_t* out, uint64_t n, const uint64_t* t, uint64_t nt, uint32_t* scratch, int* err,
+                     cudaStream_t st);
+
 }  // namespace precgpu

@@ -202,6 +202,8 @@ struct Ctx {
     size_t ws_cap = 0;
     uint64_t* io = nullptr;
     size_t io_cap = 0;  // limbs
+    uint64_t* blk = nullptr;  // blocked products: a block pair's product, then the add kernel's scratch
+    size_t blk_cap = 0;       // limbs
     int* d_err = nullptr;      // device status: error bits at +0, FFT max distance at +8
     int* h_err = nullptr;      // pinned copy of the status
     double* d_maxdist = nullptr;
@@ -408,6 +410,22 @@ static int ensure_ws(Ctx& c, size_t bytes) {
     return 0;
 }
 
+static int ensure_blk(Ctx& c, size_t limbs) {
+    if (limbs <= c.blk_cap) return 0;
+    if (c.blk) {
+        CK(cudaDeviceSynchronize());
+        cudaFree(c.blk);
+        c.blk = nullptr;
+        c.blk_cap = 0;
+    }
+    if (cudaMalloc(&c.blk, limbs * sizeof(uint64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return PREC_GPU_E_NOMEM;
+    }
+    c.blk_cap = limbs;
+    return 0;
+}
+
 static int ensure_io(Ctx& c, size_t limbs) {
     if (limbs <= c.io_cap) return 0;
     if (c.io) {
@@ -470,6 +488,62 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         const bool split = c.split_primes && pl.split;
         ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready);
     }
+    CK(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Blocked products: operands above the block size B (default 2^24 limbs,
+// the size above which the reference's mul_ntt hands a product to mul_fft,
+// src/mul_ntt.cpp:494-518) are cut into blocks of at most B limbs; every
+// pair of blocks is one NTT-band product into a temporary, added into the
+// result at its limb offset by k_add_into (ntt_add.cu).  All on one stream.
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t kDefaultBlockLimbs = 1ull << 24;
+constexpr uint64_t kMinBlockLimbs = 1024;
+static std::atomic<uint64_t> g_block_limbs{kDefaultBlockLimbs};
+
+static uint64_t block_limbs() { return g_block_limbs.load(std::memory_order_relaxed); }
+
+// Device memory of a blocked product (the workspace of every block shape --
+// whole blocks and the remainders -- and the temporary); `top` gets the
+// plan of a whole block pair.
+static int prepare_blocked(Ctx& c, uint64_t la, uint64_t lb, uint64_t B, Plan& top) {
+    const uint64_t sa[2] = {std::min(B, la), la % B}, sb[2] = {std::min(B, lb), lb % B};
+    size_t ws = 0;
+    for (int x = 0; x < 2; ++x)
+        for (int y = 0; y < 2; ++y) {
+            if (!sa[x] || !sb[y]) continue;
+            Plan pl;
+            int r = plan_for(2 * sa[x], 2 * sb[y], sa[x] + sb[y], pl, wide_digits());
+            if (r) return r;
+            ws = std::max(ws, pl.work_bytes);
+            if (x == 0 && y == 0) top = pl;
+        }
+    const uint64_t tl = sa[0] + sb[0];
+    int r = ensure_ws(c, ws);
+    if (!r) r = ensure_blk(c, tl + (add_into_scratch_words(tl) + 1) / 2);
+    return r;
+}
+
+// Enqueues a blocked product (after prepare_blocked for the same sizes).
+static int enqueue_blocked(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
+                           uint64_t* d_out, cudaStream_t st, uint64_t B) {
+    const uint64_t lout = la + lb;
+    const uint64_t tl = std::min(B, la) + std::min(B, lb);
+    uint64_t* tmp = c.blk;
+    uint32_t* scratch = reinterpret_cast<uint32_t*>(c.blk + tl);
+    int r = 0;
+    CK(cudaMemsetAsync(d_out, 0, lout * sizeof(uint64_t), st));
+    for (uint64_t i = 0; i < la; i += B)
+        for (uint64_t j = 0; j < lb; j += B) {
+            const uint64_t na = std::min(B, la - i), nb = std::min(B, lb - j);
+            Plan pl;
+            if ((r = plan_for(2 * na, 2 * nb, na + nb, pl, wide_digits()))) return r;
+            if ((r = enqueue_ntt(c, d_a + i, na, d_b + j, nb, tmp, pl, st))) return r;
+            launch_add_into(d_out + i + j, lout - i - j, tmp, na + nb, scratch, c.d_err, st);
+        }
     CK(cudaGetLastError());
     return 0;
 }
@@ -574,9 +648,17 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     FftPlan fp;
     const bool use_fft = ((mode == kModeBands && hi > kFftBandMin) || mode == kModeFft) && hi <= kFftBandMax &&
                          fft_plan_for(la, lb, fp);
+    // operands above the block size: a blocked product (the reference's
+    // mul_ntt passes them to mul_fft, src/mul_ntt.cpp:494-518)
+    const uint64_t B = block_limbs();
+    const bool blocked = !use_fft && hi > B;
     Plan pl;
-    if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl, wide_digits()))) return r;
-    if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
+    if (blocked) {
+        if ((r = prepare_blocked(c, la, lb, B, pl))) return r;
+    } else {
+        if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl, wide_digits()))) return r;
+        if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
+    }
     // operands and result each start on a 256-byte boundary (32 limbs)
     const size_t la_pad = (la + 31) & ~(size_t)31, lb_pad = square ? 0 : (lb + 31) & ~(size_t)31;
     if ((r = ensure_io(c, la_pad + lb_pad + lout))) return r;
@@ -613,6 +695,8 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         f.k2 = fp.k2;
         fft_launch(f, st);
         CK(cudaGetLastError());
+    } else if (blocked) {
+        if ((r = enqueue_blocked(c, d_a, la, d_b, lb, d_out, st, B))) return r;
     } else if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st, nullptr, c.ev_a, c.ev_b))) {
         return r;
     }
@@ -627,7 +711,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     CK(cudaStreamSynchronize(st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
-    t_stats.path = use_fft ? 2 : pl.path;
+    t_stats.path = use_fft ? 2 : (blocked ? 3 : pl.path);
     t_stats.log2_n = use_fft ? fp.k : pl.k;
     t_stats.primes = use_fft ? 0 : pl.nprimes;
     t_stats.digit_bits = use_fft ? fp.b : (pl.set == kWideSet ? 64 : 32);
@@ -713,6 +797,14 @@ int prec_gpu_mul_device(const uint64_t* d_a, size_t an, const uint64_t* d_b, siz
     if (r) return r;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Plan pl;
+    const uint64_t B = block_limbs();
+    if (an > B || bn > B) {
+        if ((r = prepare_blocked(c, an, bn, B, pl))) return r;
+        CK(cudaStreamWaitEvent(st, c.last_done, 0));
+        if ((r = enqueue_blocked(c, d_a, an, d_b, bn, d_out, st, B))) return r;
+        CK(cudaEventRecord(c.last_done, st));
+        return 0;
+    }
     if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits()))) return r;
     if ((r = ensure_ws(c, pl.work_bytes))) return r;
     CK(cudaStreamWaitEvent(st, c.last_done, 0));
@@ -770,6 +862,12 @@ int prec_gpu_last_stats(prec_gpu_stats_t* st) {
 
 uint64_t prec_gpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+size_t prec_gpu_set_block_limbs(size_t limbs) {
+    uint64_t v = limbs == 0 ? kDefaultBlockLimbs : limbs;
+    v = std::max(kMinBlockLimbs, std::min(kDefaultBlockLimbs, v));
+    return (size_t)g_block_limbs.exchange(v, std::memory_order_relaxed);
+}
+
 int prec_gpu_set_wide_digits(int on) {
     const int prev = wide_digits() ? 1 : 0;
     g_wide.store(on ? 1 : 0, std::memory_order_relaxed);
@@ -777,7 +875,7 @@ int prec_gpu_set_wide_digits(int on) {
 }
 
 int prec_gpu_ntt_log2(size_t an, size_t bn) {
-    if (an == 0 || bn == 0) return 0;
+    if (an == 0 || bn == 0 || an > block_limbs() || bn > block_limbs()) return 0;
     Plan pl;
     if (plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits())) return 0;
     return pl.k;

@@ -28,6 +28,7 @@ EXPORTS = (
     "prec_gpu_serve_wait", "prec_gpu_serve_drain", "prec_gpu_serve_stats", "prec_gpu_serve_destroy",
     "prec_gpu_sqr", "prec_gpu_autotune", "prec_gpu_tune_get", "prec_gpu_tune_set", "prec_gpu_tune_reset",
     "prec_gpu_tune_save", "prec_gpu_tune_load", "prec_gpu_launch_count", "prec_gpu_set_wide_digits",
+    "prec_gpu_set_block_limbs",
 )
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -93,6 +94,8 @@ def lib() -> ctypes.CDLL:
         L.prec_gpu_launch_count.restype = ctypes.c_uint64
         L.prec_gpu_set_wide_digits.argtypes = [ctypes.c_int]
         L.prec_gpu_set_wide_digits.restype = ctypes.c_int
+        L.prec_gpu_set_block_limbs.argtypes = [ctypes.c_size_t]
+        L.prec_gpu_set_block_limbs.restype = ctypes.c_size_t
         L.prec_gpu_autotune.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneEntry), ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t)]
         L.prec_gpu_autotune.restype = ctypes.c_int
@@ -214,6 +217,12 @@ def autotune(kmin: int = 13, kmax: int = 26):
 def launch_count() -> int:
     """Kernel launches the library has issued in this process."""
     return int(lib().prec_gpu_launch_count())
+
+
+def set_block_limbs(limbs: int) -> int:
+    """Block size (limbs) above which a product runs blocked (0: the default,
+    2^24); returns the previous setting."""
+    return int(lib().prec_gpu_set_block_limbs(limbs))
 
 
 def set_wide_digits(on: bool) -> bool:

@@ -87,3 +87,26 @@ def test_no_device_fails_loudly():
     assert rc == native.E_NODEV
     with pytest.raises(native.PrecGpuError):
         native.mul(np.ones(3, np.uint64), np.ones(3, np.uint64))
+
+
+def test_block_limbs():
+    """Products with an operand above the block size run blocked (no single
+    transform length); the size is clamped to [1024, 2^24]."""
+    prev = native.set_block_limbs(4096)
+    try:
+        assert native.ntt_log2(4097, 10) == 0
+        assert native.ntt_log2(4096, 4096) > 0
+        assert native.set_block_limbs(10) == 4096
+        assert native.set_block_limbs(0) == 1024
+        assert native.set_block_limbs(1 << 30) == 1 << 24
+        assert native.ntt_log2((1 << 24) + 1, 5) == 0
+        assert native.ntt_log2(1 << 24, 5) > 0
+    finally:
+        native.set_block_limbs(prev)
+
+
+def test_noalloc_rejects_oversize():
+    """The no-allocation entry point refuses more than 131072 limbs from the
+    sizes alone, before any CUDA call (so this runs without a device)."""
+    rc = native.lib().prec_gpu_mul_device_noalloc(1, 65537, 1, 65536, 1, None)
+    assert rc == native.E_TOO_LARGE

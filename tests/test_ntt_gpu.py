@@ -179,16 +179,6 @@ def test_device_api_odd_limb_offsets(gpu):
         assert np.array_equal(got, O.mul_ntt(a, b)), (an, bn)
 
 
-def test_too_large_rejected(gpu):
-    a = np.ones(1, np.uint64)
-    with pytest.raises(gpu.PrecGpuError) as e:
-        # 2^25 + 1 total limbs exceed the 2^26-point transform; no allocation happens
-        gpu.lib().prec_gpu_mul_device  # noqa: B018
-        code = gpu.lib().prec_gpu_mul_device(1, (1 << 24) + 1, 1, 1 << 24, 1, None)
-        gpu.check(code)
-    assert e.value.code == gpu.E_TOO_LARGE
-
-
 def test_host_api_pinned_result_buffer(gpu):
     """Page-locked operand and result buffers: the limbs, nothing written
     past an + bn, and a result written over its own operand."""

@@ -38,11 +38,3 @@ def test_noalloc_matches_allocating_entry_point():
             assert rc == native.OK, native.strerror(rc)
             torch.cuda.synchronize()
             assert torch.equal(got, want), (an, bn, call)
-
-
-def test_noalloc_rejects_oversize():
-    from preclib_gb300 import native
-    L = native.lib()
-    # 131073 limbs in total exceed the fixed scratch; refused before any device work
-    rc = L.prec_gpu_mul_device_noalloc(1, 65537, 1, 65536, 1, None)
-    assert rc == native.E_TOO_LARGE

@@ -28,20 +28,29 @@ struct Coef3 {
 
 // Garner over the five primes (the constants of Crt5Const) from the
 // inverse-transform outputs y_j (any value below 2^32 of each class), then
-// c = v0 + p0 (v1 + p1 (v2 + p2 (v3 + p3 v4))).
+// c = v0 + p0 (v1 + p1 (v2 + p2 (v3 + p3 v4))).  LAZY (set 2, p < 2^30):
+// running values in [0, 2p); otherwise (set 3, p < 2^31) in [0, p).
+template <bool LAZY>
 __device__ __forceinline__ Coef3 crt5(const uint32_t (&y)[5], const Crt5Const& cc, const FieldArgs& f) {
     uint32_t v[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
         const uint32_t p = f.pc[j].p, p2 = f.pc[j].p2;
-        uint32_t acc = shoup_lazy(y[j], cc.a[j].w, cc.a[j].wp, p);  // [0, 2p)
+        if constexpr (LAZY) {
+            uint32_t acc = shoup_lazy(y[j], cc.a[j].w, cc.a[j].wp, p);  // [0, 2p)
 #pragma unroll
-        for (int i = 0; i < j; ++i) {
-            const ShoupC b = cc.b[j * (j - 1) / 2 + i];
-            const uint32_t t = acc + p2 - shoup_lazy(v[i], b.w, b.wp, p);  // (0, 4p)
-            acc = min(t, t - p2);
+            for (int i = 0; i < j; ++i) {
+                const ShoupC b = cc.b[j * (j - 1) / 2 + i];
+                const uint32_t t = acc + p2 - shoup_lazy(v[i], b.w, b.wp, p);  // (0, 4p)
+                acc = min(t, t - p2);
+            }
+            v[j] = red1(acc, p);
+        } else {
+            uint32_t acc = shoup_mul(y[j], cc.a[j], p);  // [0, p)
+#pragma unroll
+            for (int i = 0; i < j; ++i) acc = sub_mod(acc, shoup_mul(v[i], cc.b[j * (j - 1) / 2 + i], p), p);
+            v[j] = acc;
         }
-        v[j] = red1(acc, p);
     }
     u128 X = (u128)((uint64_t)v[4] * f.pc[3].p + v[3]);
     X = X * f.pc[2].p + v[2];
@@ -55,13 +64,14 @@ __device__ __forceinline__ Coef3 crt5(const uint32_t (&y)[5], const Crt5Const& c
     return c;
 }
 
+template <bool LAZY>
 __device__ __forceinline__ Coef3 coef5(const uint32_t* __restrict__ work, uint64_t N, int64_t i,
                                        const ProdArgs& args) {
     if (i < 0 || (uint64_t)i >= N) return Coef3{0, 0, 0};
     uint32_t y[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) y[j] = work[(uint64_t)(2 * j) * N + i];
-    return crt5(y, args.crt5, args.f);
+    return crt5<LAZY>(y, args.crt5, args.f);
 }
 
 // sum of limb m: S_m = w0(c_m) + w1(c_(m-1)) + w2(c_(m-2)) < 2^66
@@ -79,6 +89,7 @@ struct WideEdge {
 // first limbs need from below come from the lane below, from the warp
 // below (shared memory), or for the block's first thread from three
 // coefficients computed again by lanes 0..2 of warp 0.
+template <bool LAZY>
 __device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& args, int64_t m0, u128 (&T)[kCarryLimbs],
                                           uint64_t& prev_hi, WideEdge* s_edge) {
     static_assert(kCarryLimbs >= 4 && kCarryLimbs % 4 == 0, "limbs per thread: whole 16-byte loads");
@@ -96,20 +107,20 @@ __device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& ar
             uint32_t y[5];
 #pragma unroll
             for (int j = 0; j < 5; ++j) y[j] = r[j].x;
-            c[4 * h] = crt5(y, args.crt5, args.f);
+            c[4 * h] = crt5<LAZY>(y, args.crt5, args.f);
 #pragma unroll
             for (int j = 0; j < 5; ++j) y[j] = r[j].y;
-            c[4 * h + 1] = crt5(y, args.crt5, args.f);
+            c[4 * h + 1] = crt5<LAZY>(y, args.crt5, args.f);
 #pragma unroll
             for (int j = 0; j < 5; ++j) y[j] = r[j].z;
-            c[4 * h + 2] = crt5(y, args.crt5, args.f);
+            c[4 * h + 2] = crt5<LAZY>(y, args.crt5, args.f);
 #pragma unroll
             for (int j = 0; j < 5; ++j) y[j] = r[j].w;
-            c[4 * h + 3] = crt5(y, args.crt5, args.f);
+            c[4 * h + 3] = crt5<LAZY>(y, args.crt5, args.f);
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < L; ++k) c[k] = coef5(PP.work, N, m0 + k, args);
+        for (int k = 0; k < L; ++k) c[k] = coef5<LAZY>(PP.work, N, m0 + k, args);
     }
     const u128 s_last = limb_sum(c[L - 1], c[L - 2].w1, c[L - 3].w2);
     const uint32_t hi_last = (uint32_t)(s_last >> 64);
@@ -123,7 +134,7 @@ __device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& ar
         // the block's first limb: coefficients m0-1, m0-2, m0-3 (lanes 0, 1, 2)
         Coef3 e = Coef3{0, 0, 0};
         const int64_t mb = m0 - lane * L;  // the block's first limb
-        if (lane < 3) e = coef5(PP.work, N, mb - 1 - lane, args);
+        if (lane < 3) e = coef5<LAZY>(PP.work, N, mb - 1 - lane, args);
         const uint64_t e1w0 = __shfl_sync(0xffffffffu, e.w0, 0);
         const uint64_t e1w1 = __shfl_sync(0xffffffffu, e.w1, 0);
         const uint32_t e1w2 = __shfl_sync(0xffffffffu, e.w2, 0);
@@ -168,8 +179,8 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
 
     u128 T[kCarryLimbs];
     uint64_t prev_hi = 0;
-    if constexpr (SET == kWideSet) {
-        wide_sums(PP, args, m0, T, prev_hi, s_edge);
+    if constexpr (set_wide(SET)) {
+        wide_sums<SET == kWideSet>(PP, args, m0, T, prev_hi, s_edge);
     } else {
         const uint32_t* __restrict__ r0 = PP.work;
         const uint32_t* __restrict__ r1 = PP.work + 2 * N;
@@ -269,7 +280,8 @@ void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtr
     const dim3 grid(batch ? max_nblk : a.nblk, 1, count);
     if (set == 0) k_crt_carry<0><<<grid, kCarryThreads, 0, st>>>(a, batch);
     else if (set == 1) k_crt_carry<1><<<grid, kCarryThreads, 0, st>>>(a, batch);
-    else k_crt_carry<kWideSet><<<grid, kCarryThreads, 0, st>>>(a, batch);
+    else if (set == kWideSet) k_crt_carry<kWideSet><<<grid, kCarryThreads, 0, st>>>(a, batch);
+    else k_crt_carry<kWideSetL><<<grid, kCarryThreads, 0, st>>>(a, batch);
     count_launches(1);
 }
 

@@ -42,7 +42,7 @@ __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __
 #pragma unroll
         for (int q = 0; q < H; ++q) {
             uint32_t d;
-            if constexpr (SET == kWideSet) d = Ar<SET>::digit64(s[q * G::QS * C], s[(q + H) * G::QS * C], c);
+            if constexpr (set_wide(SET)) d = Ar<SET>::digit64(s[q * G::QS * C], s[(q + H) * G::QS * C], c);
             else d = Ar<SET>::digit(s[q * G::QS * C], c);
             const uint2 wq = __ldg(&tw[(1u << (G::LO + G::RB - 1)) + (ulo | ((uint32_t)q << G::LO))]);
             x[0][q] = d;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
             P.scratch[i] = 0;
     }
 
-    if constexpr (SET == kWideSet) {
+    if constexpr (set_wide(SET)) {
         // one digit per limb; the plan puts both operands in the lower half
         const uint64_t nl = operand ? P.lb : P.la;
         if (nl > (1ull << (args.k - 1))) {
@@ -173,14 +173,16 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args,
     X(0, 6, 4, 6) X(0, 6, 8, 6) X(0, 7, 4, 6) X(0, 7, 8, 6) X(0, 8, 4, 6) X(0, 8, 8, 6) X(0, 9, 4, 6)     \
     X(0, 9, 8, 6) X(0, 10, 4, 4) X(0, 10, 8, 4) X(0, 10, 4, 6) X(0, 10, 8, 6) X(0, 11, 4, 4)              \
     X(0, 11, 8, 4) X(0, 11, 4, 6) X(0, 11, 8, 6) X(1, 11, 4, 4) X(1, 11, 8, 4) X(1, 11, 4, 6)             \
-    X(1, 11, 8, 6) X(1, 12, 4, 6) X(1, 13, 4, 6)
+    X(1, 11, 8, 6) X(1, 12, 4, 6) X(1, 13, 4, 6) X(1, 10, 4, 6) X(1, 10, 8, 6)
 
-// the forward column kernel of set 2 (64-bit digits) in the same (M, C, MR)
-// configurations as set 0; its other kernels are set 0's
+// the forward column kernels of sets 2 and 3 (64-bit digits) in the
+// (M, C, MR) configurations of sets 0 and 1; their other kernels are set 0's
+// and set 1's
 #define PREC_COLS_WIDE_CONFIGS(X)                                                                       \
     X(2, 6, 4, 6) X(2, 6, 8, 6) X(2, 7, 4, 6) X(2, 7, 8, 6) X(2, 8, 4, 6) X(2, 8, 8, 6) X(2, 9, 4, 6)     \
     X(2, 9, 8, 6) X(2, 10, 4, 4) X(2, 10, 8, 4) X(2, 10, 4, 6) X(2, 10, 8, 6) X(2, 11, 4, 4)              \
-    X(2, 11, 8, 4) X(2, 11, 4, 6) X(2, 11, 8, 6)
+    X(2, 11, 8, 4) X(2, 11, 4, 6) X(2, 11, 8, 6) X(3, 10, 4, 6) X(3, 10, 8, 6) X(3, 11, 4, 4)             \
+    X(3, 11, 8, 4) X(3, 11, 4, 6) X(3, 11, 8, 6) X(3, 12, 4, 6)
 
 inline size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
 

@@ -7,7 +7,7 @@ namespace precgpu {
 void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
     if (nprimes <= 0) nprimes = kSetPrimes[set];
     int cg, mr;
-    col_config(set == kWideSet ? 0 : set, a.k1, a.cg, a.cmr, cg, mr);
+    col_config(set_base(set), a.k1, a.cg, a.cmr, cg, mr);
     const dim3 grid((1u << a.k2) / cg, (a.square || a.operand_only ? 1 : 2) * nprimes, count);
     const size_t smem = col_smem(a.k1, cg);
 #define X(S, MM, CC, RR)                                                     \

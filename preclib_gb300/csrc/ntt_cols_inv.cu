@@ -6,7 +6,7 @@ namespace precgpu {
 
 void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
     if (nprimes <= 0) nprimes = kSetPrimes[set];
-    if (set == kWideSet) set = 0;  // the same kernel on set 2's residues
+    set = set_base(set);  // sets 2 and 3: the same kernel on their residues
     int cg, mr;
     col_config(set, a.k1, a.cg, a.cmr, cg, mr);
     const dim3 grid((1u << a.k2) / cg, nprimes, count);

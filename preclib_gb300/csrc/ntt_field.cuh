@@ -24,6 +24,11 @@
 //        operands in the lower half guarantee.  Half the points of a 32-bit
 //        digit transform: 5 transforms of N/2 points per operand instead of
 //        3 of N, about 17% fewer butterflies.
+//  set 3 (2^23 .. 2^25 points, digits = 64-bit limbs): 2113929217 =
+//        63*2^25+1, 2013265921, 1811939329, 1711276033 = 51*2^25+1,
+//        1107296257 = 33*2^25+1; generators 5, 31, 13, 29, 10.  Above 2^30:
+//        set 1's reduced arithmetic.  The product ~2^153.36 exceeds
+//        42941745 * (2^64-1)^2 >= min(la, lb) (2^24 at most) * (2^64-1)^2.
 //
 // Multiplication methods (all on the 32-bit integer pipes):
 //  * Shoup's precomputed-quotient product for twiddles known in advance:
@@ -39,11 +44,17 @@ namespace precgpu {
 
 constexpr int kPrimes = 3;     // primes of sets 0 and 1
 constexpr int kMaxPrimes = 5;  // primes of set 2
-constexpr int kSets = 3;
-constexpr int kSetMaxLog2[kSets] = {23, 26, 22};  // 2-adicity cap of each set
-constexpr int kSetPrimes[kSets] = {3, 3, 5};
-constexpr int kMaxLog2 = 26;                      // longest transform of any set
-constexpr int kWideSet = 2;                       // the set of 64-bit digits
+constexpr int kSets = 4;
+constexpr int kSetMaxLog2[kSets] = {23, 26, 22, 25};  // 2-adicity cap of each set
+constexpr int kSetPrimes[kSets] = {3, 3, 5, 5};
+constexpr int kMaxLog2 = 26;                          // longest transform of any set
+constexpr int kWideSet = 2;                           // 64-bit digits up to 2^22 points (set 0's arithmetic)
+constexpr int kWideSetL = 3;                          // 64-bit digits, 2^23 .. 2^25 points (set 1's arithmetic)
+
+// 64-bit digits over five primes
+__host__ __device__ constexpr bool set_wide(int s) { return s >= kWideSet; }
+// the three-prime set whose arithmetic and row / inverse-column kernels a set shares
+__host__ __device__ constexpr int set_base(int s) { return s >= kWideSet ? s - kWideSet : s; }
 constexpr int kMaxSubLog2 = 13;               // largest shared-memory sub-transform
 constexpr int kTwLevelBits = 13;              // low level of the four-step twiddle table
 
@@ -190,6 +201,16 @@ struct Ar<1> {
         return red1(shoup_lazy(x, w.x, w.y, c.p), c.p);
     }
     static __device__ __forceinline__ uint32_t half(uint32_t x, const PrimeC&) { return x; }
+};
+
+// set 3: set 1's arithmetic; a digit is a whole 64-bit limb hi*2^32 + lo
+template <>
+struct Ar<3> : Ar<1> {
+    static __device__ __forceinline__ uint32_t digit64(uint32_t lo, uint32_t hi, const PrimeC& c) {
+        const uint32_t l = red1(lo - __umulhi(lo, c.one_wp) * c.p, c.p);    // [0, p)
+        const uint32_t h = red1(shoup_lazy(hi, c.r32, c.r32p, c.p), c.p);  // [0, p)
+        return red1(l + h, c.p);                                             // l + h < 2p < 2^32
+    }
 };
 
 #endif  // __CUDACC__

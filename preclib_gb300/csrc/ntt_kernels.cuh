@@ -162,8 +162,8 @@ int ntt_configure_kernels();  // opt-in shared-memory sizes; returns a cudaError
 
 // launchers of each translation unit (ntt_cols.cu, ntt_rows.cu, ntt_carry.cu, ntt_small.cu)
 // (primes a.prime0 .. a.prime0 + nprimes - 1; 0 = every prime of the set).
-// The row and inverse column kernels of set 2 are set 0's: the same
-// arithmetic on residues, with set 2's primes and tables in a.f.
+// The row and inverse column kernels of sets 2 and 3 are those of sets 0
+// and 1: the same arithmetic on residues, with their primes and tables in a.f.
 void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
                      int nprimes = 0);
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
@@ -189,6 +189,7 @@ inline int row_radix_cap(int m, int req) {
 }
 
 inline void col_config(int set, int m, int req_cg, int req_mr, int& cg, int& mr) {
+    set = set_base(set);
     cg = (req_cg == 4 || req_cg == 8) ? req_cg : kColGroup;
     if (set == 1 && m >= 12) cg = 4;
     mr = (m == 10 || m == 11) && req_mr == 4 ? 4 : 6;

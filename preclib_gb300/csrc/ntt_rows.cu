@@ -158,7 +158,7 @@ int ntt_row_threads(int k2, int n1, int* rows_out) {
 
 void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int nprimes) {
     if (nprimes <= 0) nprimes = kSetPrimes[set];
-    if (set == kWideSet) set = 0;  // the same kernel on set 2's residues
+    set = set_base(set);  // sets 2 and 3: the same kernel on their residues
     const int m = a.k2;
     const dim3 grid((1u << a.k1) / a.rows, nprimes, count);
     const int threads = a.rows << (m - 5);

@@ -186,7 +186,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
                 batch_free(b);
                 return r;
             }
-            if (c.pl.k != k || (c.pl.set == kWideSet) != (kw != 0)) {  // the key and the plan agree
+            if (c.pl.k != k || set_wide(c.pl.set) != (kw != 0)) {  // the key and the plan agree
                 batch_free(b);
                 return PREC_GPU_E_INTERNAL;
             }
@@ -207,7 +207,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
         if (c.pl.path == 1) {
             // a product of 2^k points has at most 2^(k-1) + 1 limbs on 32-bit
             // digits, 2^k + 1 on 64-bit digits
-            const uint64_t lout_max = c.pl.set == kWideSet ? (1ull << c.k) + 1 : (1ull << c.k) / 2 + 1;
+            const uint64_t lout_max = set_wide(c.pl.set) ? (1ull << c.k) + 1 : (1ull << c.k) / 2 + 1;
             const size_t carry_words = (size_t)(lout_max / (kCarryThreads * kCarryLimbs)) + 2;
             c.ws_per = align256(((size_t)2 * c.pl.nprimes << c.k) * sizeof(uint32_t) + carry_words * sizeof(uint32_t));
             c.per_chunk = (int)std::min<size_t>({n, std::max<size_t>(1, budget / c.ws_per), 65535});

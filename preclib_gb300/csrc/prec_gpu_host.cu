@@ -30,14 +30,18 @@ typedef unsigned __int128 u128;
 
 // Prime sets (see ntt_field.cuh): set 0 for transforms up to 2^23 points,
 // set 1 -- the reference's primes and generators, src/mul_ntt.cpp:29-34 --
-// for 2^24 .. 2^26 points, set 2 (five primes, 64-bit digits) up to 2^22.
-static const uint32_t kP[kSets][kMaxPrimes] = {{998244353u, 897581057u, 880803841u},
-                                               {469762049u, 1811939329u, 2013265921u},
-                                               {998244353u, 985661441u, 943718401u, 935329793u, 918552577u}};
-static const uint32_t kG[kSets][kMaxPrimes] = {{3u, 3u, 26u}, {3u, 13u, 31u}, {3u, 3u, 7u, 3u, 5u}};
-// set 2 recovers every coefficient exactly while min(la, lb) stays below
-// p1..p5 / (2^64 - 1)^2 = 2344425.6
-constexpr uint64_t kWideMaxMinLimbs = 2344425;
+// for 2^24 .. 2^26 points; sets 2 and 3 (five primes, 64-bit digits) up to
+// 2^22 and for 2^23 .. 2^25 points.
+static const uint32_t kP[kSets][kMaxPrimes] = {
+    {998244353u, 897581057u, 880803841u},
+    {469762049u, 1811939329u, 2013265921u},
+    {998244353u, 985661441u, 943718401u, 935329793u, 918552577u},
+    {2113929217u, 2013265921u, 1811939329u, 1711276033u, 1107296257u}};
+static const uint32_t kG[kSets][kMaxPrimes] = {
+    {3u, 3u, 26u}, {3u, 13u, 31u}, {3u, 3u, 7u, 3u, 5u}, {5u, 31u, 13u, 29u, 10u}};
+// a five-prime set recovers every coefficient exactly while min(la, lb)
+// stays below p1..p5 / (2^64 - 1)^2: 2344425.6 (set 2), 42941745.4 (set 3)
+static uint64_t wide_max_min_limbs(int set) { return set == kWideSet ? 2344425ull : 42941745ull; }
 
 static uint32_t powmod(uint64_t b, uint64_t e, uint32_t m) {
     uint64_t r = 1 % m;
@@ -105,8 +109,8 @@ static CrtConst crt_compute(int set, int k) {
 // Garner constants of set 2 for 2^k points (Crt5Const): scale
 // s_j = 2^32 N^-1 (the Montgomery factor of the pointwise product and the
 // inverse transform's 1/N) folded into a_j.
-static Crt5Const crt5_compute(int k) {
-    const uint32_t* P = kP[kWideSet];
+static Crt5Const crt5_compute(int set, int k) {
+    const uint32_t* P = kP[set];
     Crt5Const c;
     for (int j = 0; j < 5; ++j) {
         const uint32_t p = P[j];
@@ -135,13 +139,14 @@ static CrtConst crt_for(int set, int k) {
     return table[set][k];
 }
 
-static Crt5Const crt5_for(int k) {
-    static Crt5Const table[kMaxLog2 + 1];
+static Crt5Const crt5_for(int set, int k) {
+    static Crt5Const table[2][kMaxLog2 + 1];
     static std::once_flag once;
     std::call_once(once, [] {
-        for (int j = kSmallMaxLog2 + 1; j <= kSetMaxLog2[kWideSet]; ++j) table[j] = crt5_compute(j);
+        for (int s = kWideSet; s < kSets; ++s)
+            for (int j = kSmallMaxLog2 + 1; j <= kSetMaxLog2[s]; ++j) table[s - kWideSet][j] = crt5_compute(s, j);
     });
-    return table[k];
+    return table[set - kWideSet][k];
 }
 
 static int ceil_log2(uint64_t n) {
@@ -150,11 +155,14 @@ static int ceil_log2(uint64_t n) {
     return k;
 }
 
+int wide_set(int kw) { return kw <= kSetMaxLog2[kWideSet] ? kWideSet : kWideSetL; }
+
 int wide_log2(uint64_t la, uint64_t lb, int k32) {
     if (k32 <= kSmallMaxLog2) return 0;
     const int kw = ceil_log2(la + lb - 1);
+    if (kw <= kSmallMaxLog2 || kw > kSetMaxLog2[kWideSetL]) return 0;
     const uint64_t hi = la > lb ? la : lb, lo = la > lb ? lb : la;
-    if (kw > kSmallMaxLog2 && kw <= kSetMaxLog2[kWideSet] && 2 * hi <= (1ull << kw) && lo <= kWideMaxMinLimbs &&
+    if (2 * hi <= (1ull << kw) && lo <= wide_max_min_limbs(wide_set(kw)) &&
         5 * ((uint64_t)kw << kw) < 3 * ((uint64_t)k32 << k32))
         return kw;
     return 0;
@@ -180,12 +188,12 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
         if (kw) {
             k = kw;
             pl.k = k;
-            pl.set = kWideSet;
+            pl.set = wide_set(kw);
             pl.nprimes = kMaxPrimes;
-            pl.crt5 = crt5_for(k);
+            pl.crt5 = crt5_for(pl.set, k);
         }
     }
-    apply_config(pl, tuned_config(k));
+    apply_config(pl, config_for(k, pl.set));
     const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
     pl.nblk = (int)((lout + bl - 1) / bl);
     pl.work_bytes = ((size_t)2 * pl.nprimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
@@ -714,7 +722,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     t_stats.path = use_fft ? 2 : (blocked ? 3 : pl.path);
     t_stats.log2_n = use_fft ? fp.k : pl.k;
     t_stats.primes = use_fft ? 0 : pl.nprimes;
-    t_stats.digit_bits = use_fft ? fp.b : (pl.set == kWideSet ? 64 : 32);
+    t_stats.digit_bits = use_fft ? fp.b : (set_wide(pl.set) ? 64 : 32);
     t_stats.device_ms = ms;
     t_stats.fft_max_distance = use_fft ? *c.h_maxdist : 0.0;
     if (fft_failed) return PREC_GPU_E_FFT_ROUNDING;

@@ -37,11 +37,13 @@ struct Plan {
 // products, the batch form and the serving loop pass wide_digits(), the
 // autotuner keeps 32-bit digits.
 int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide = false);
-// log2 of the 64-bit-digit (set 2) transform for la x lb limbs, or 0 where
-// the 32-bit plan of 2^k32 points stays: set 2 needs 2^13 .. 2^22 points,
-// both operands in the lower half, min(la, lb) within the five primes'
-// bound, and fewer butterflies (5 N' log N' < 3 N log N)
+// log2 of the 64-bit-digit transform for la x lb limbs, or 0 where the
+// 32-bit plan of 2^k32 points stays: it needs 2^13 .. 2^25 points, both
+// operands in the lower half, min(la, lb) within the five primes' bound,
+// and fewer butterflies (5 N' log N' < 3 N log N)
 int wide_log2(uint64_t la, uint64_t lb, int k32);
+// the five-prime set of a 64-bit-digit transform of 2^kw points (2 or 3)
+int wide_set(int kw);
 // 64-bit digits allowed (prec_gpu_set_wide_digits; PREC_GPU_WIDE_DIGITS)
 bool wide_digits();
 
@@ -56,6 +58,10 @@ struct KernelConfig {
     int split = 0;  // per-prime stream chains
 };
 KernelConfig default_config(int k);
+// the configuration of length 2^k for a prime set: the table's (tuned or
+// default) where the length's own set shares the set's kernels, else the
+// default configuration of the set's kernel family
+KernelConfig config_for(int k, int set);
 bool config_valid(int k, const KernelConfig& c);
 // the table's configuration for length 2^k (k >= 13)
 KernelConfig tuned_config(int k);

@@ -46,9 +46,8 @@ bool pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
 
 }  // namespace
 
-KernelConfig default_config(int k) {
+static KernelConfig default_config_set(int k, int set) {
     KernelConfig c;
-    const int set = set_of(k);
     // column length N1 = 2^k1, row length N2 = 2^k2; set 1 keeps the rows at
     // 2^13 so its column CTAs stay within a third of shared memory
     c.k1 = set == 0 ? k / 2 : k - 13;
@@ -61,6 +60,8 @@ KernelConfig default_config(int k) {
     c.split = k >= kSplitMinLog2 ? 1 : 0;
     return c;
 }
+
+KernelConfig default_config(int k) { return default_config_set(k, set_of(k)); }
 
 bool config_valid(int k, const KernelConfig& c) {
     if (k < kTuneMin || k > kTuneMax) return false;
@@ -86,6 +87,11 @@ KernelConfig tuned_config(int k) {
         if (g_tune[k].tuned) return g_tune[k].cfg;
     }
     return default_config(k);
+}
+
+KernelConfig config_for(int k, int set) {
+    const int base = set_base(set);
+    return base == set_of(k) ? tuned_config(k) : default_config_set(k, base);
 }
 
 void apply_config(Plan& pl, const KernelConfig& c) {

@@ -53,11 +53,13 @@ def test_ntt_plan_sizes():
         assert native.ntt_log2(1 << 20, 1000) == 21
         # one operand above half the 64-bit-digit transform: 32-bit digits
         assert native.ntt_log2(3 << 19, 1 << 19) == 22
-        # small transforms and beyond 2^22 points: 32-bit digits
+        # 2^23 .. 2^25 points: the second five-prime set
+        assert native.ntt_log2(1 << 22, 1 << 22) == 23
+        assert native.ntt_log2(1 << 24, 1 << 24) == 25
+        assert native.ntt_log2(3 << 22, 1 << 22) == 25  # one operand above half: 32-bit digits
+        # small transforms: 32-bit digits
         assert native.ntt_log2(1500, 1500) == 13
         assert native.ntt_log2(1, 1) == 5
-        assert native.ntt_log2(1 << 22, 1 << 22) == 24
-        assert native.ntt_log2(1 << 24, 1 << 24) == 26
     finally:
         native.set_wide_digits(prev)
 

@@ -78,9 +78,11 @@ def _spot(p, a):
 
 def test_sqr_large_both_prime_sets(gpu):
     """2^22-point (prime set 0, 32-bit digits), 2^21- and 2^22-point (set 2,
-    64-bit digits) and 2^24 / 2^25-point (prime set 1) squares."""
+    64-bit digits), 2^24 / 2^25-point (prime set 1, 32-bit digits) and
+    2^23 / 2^24-point (set 3, 64-bit digits) squares."""
     for (n, s, k, wide) in ((1 << 20, 3, 22, False), (1 << 20, 3, 21, True), (1 << 21, 6, 22, True),
-                            (3 << 20, 4, 24, True), (3 << 21, 5, 25, True)):
+                            (3 << 20, 4, 24, False), (3 << 21, 5, 25, False), (3 << 20, 4, 23, True),
+                            (3 << 21, 5, 24, True)):
         prev = gpu.set_wide_digits(wide)
         try:
             a = O.splitmix64(s, n)

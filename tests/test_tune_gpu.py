@@ -68,22 +68,29 @@ def _spot(p, a, b):
         assert O.mod_u64(p, q) == O.mod_u64(a, q) * O.mod_u64(b, q) % q
 
 
-def test_prime_set_1_configs(gpu):
-    """2^24 points (the reference's primes, rows of 2^13): every valid
-    column configuration, residue spot checks and agreement between configs."""
-    k, n = 24, 3 << 20
+@pytest.mark.parametrize("wide", [False, True])
+def test_prime_set_1_configs(gpu, wide):
+    """2^24 points, rows of 2^13: every valid column configuration on set 1
+    (the reference's primes, 32-bit digits) and on set 3 (five primes,
+    64-bit digits), residue spot checks and agreement between configs."""
+    k, n = 24, (3 << 20) if not wide else (3 << 21)
     a = O.splitmix64(91, n)
     b = O.splitmix64(92, n)
     ref = None
-    for cfg in _configs(gpu, k):
-        gpu.tune_set(**cfg)
-        p = gpu.mul(a, b, ntt=True)
-        assert gpu.last_stats().log2_n == k
-        if ref is None:
-            _spot(p, a, b)
-            ref = p
-        else:
-            assert np.array_equal(p, ref), cfg
+    prev = gpu.set_wide_digits(wide)
+    try:
+        for cfg in _configs(gpu, k):
+            gpu.tune_set(**cfg)
+            p = gpu.mul(a, b, ntt=True)
+            assert gpu.last_stats().log2_n == k
+            assert gpu.last_stats().primes == (5 if wide else 3)
+            if ref is None:
+                _spot(p, a, b)
+                ref = p
+            else:
+                assert np.array_equal(p, ref), cfg
+    finally:
+        gpu.set_wide_digits(prev)
 
 
 def test_autotune_installs_exact_configs(gpu, tmp_path):

@@ -9,6 +9,8 @@ import oracle as O
 
 pytestmark = pytest.mark.gpu
 
+B1 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
 
 def _mul(gpu, a, b, wide):
     prev = gpu.set_wide_digits(wide)
@@ -65,14 +67,28 @@ def test_random_shapes_both_widths(gpu):
 
 
 def test_large_both_widths(gpu):
-    """2^19 .. 2^22-point products: 64-bit and 32-bit digits bit for bit."""
-    for (an, bn) in ((1 << 18, 1 << 18), (3 << 18, 1 << 20), (1 << 20, 999999), (1 << 21, 1 << 21)):
+    """2^19 .. 2^24-point products (sets 2 and 3 against sets 0 and 1):
+    64-bit and 32-bit digits bit for bit."""
+    for (an, bn) in ((1 << 18, 1 << 18), (3 << 18, 1 << 20), (1 << 20, 999999), (1 << 21, 1 << 21),
+                     (1 << 22, 1 << 22), (3 << 21, 1 << 22)):
         a = O.splitmix64(an, an)
         b = O.splitmix64(bn + 3, bn)
         wide, kw = _mul(gpu, a, b, True)
         narrow, kn = _mul(gpu, a, b, False)
         assert kw == kn - 1, (an, bn)
         assert np.array_equal(wide, narrow), (an, bn)
+
+
+def test_all_ones_square_set3_bound(gpu):
+    """(2^(64n) - 1)^2 at n = 2^24 (2^25 points on set 3): the largest
+    single-transform square, coefficients up to 2^24 (2^64 - 1)^2."""
+    n = 1 << 24
+    a = np.full(n, B1)
+    got = gpu.sqr(a)
+    st = gpu.last_stats()
+    assert st.log2_n == 25 and st.primes == 5
+    assert got[0] == 1 and not got[1:n].any()
+    assert got[n] == np.uint64(0xFFFFFFFFFFFFFFFE) and (got[n + 1:] == B1).all()
 
 
 def test_all_ones_unbalanced(gpu):

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -157,10 +158,15 @@ static int ceil_log2(uint64_t n) {
 
 int wide_set(int kw) { return kw <= kSetMaxLog2[kWideSet] ? kWideSet : kWideSetL; }
 
+// Below 2^18 points the 64-bit plan measured no faster (2^13 .. 2^17: 5%
+// slower to 4% faster): those products are bound by latency and launches,
+// and five primes mean more launches.  From 2^18 it is 7-12% faster.
+constexpr int kWideMinLog2 = 18;
+
 int wide_log2(uint64_t la, uint64_t lb, int k32) {
     if (k32 <= kSmallMaxLog2) return 0;
     const int kw = ceil_log2(la + lb - 1);
-    if (kw <= kSmallMaxLog2 || kw > kSetMaxLog2[kWideSetL]) return 0;
+    if (kw < kWideMinLog2 || kw > kSetMaxLog2[kWideSetL]) return 0;
     const uint64_t hi = la > lb ? la : lb, lo = la > lb ? lb : la;
     if (2 * hi <= (1ull << kw) && lo <= wide_max_min_limbs(wide_set(kw)) &&
         5 * ((uint64_t)kw << kw) < 3 * ((uint64_t)k32 << k32))
@@ -200,6 +206,29 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
     return 0;
 }
 
+// A single four-step product up to 2^kGraphMaxLog2 points runs as one CUDA
+// graph replay: its kernels are the batch form's with a one-entry
+// descriptor array, captured once per plan shape; each call uploads the
+// descriptor (operands, output, workspace, sizes) and launches the graph.
+// Below 2^19 points the four kernels take only a few microseconds each,
+// so launching them one by one left the GPU waiting on the host.
+constexpr int kGraphMaxLog2 = 18;
+
+struct GraphKey {
+    int set, k, k1, cg, cmr, rmr, rows, square;
+    bool operator<(const GraphKey& o) const {
+        const int a[8] = {set, k, k1, cg, cmr, rmr, rows, square};
+        const int b[8] = {o.set, o.k, o.k1, o.cg, o.cmr, o.rmr, o.rows, o.square};
+        return std::lexicographical_compare(a, a + 8, b, b + 8);
+    }
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    ProdPtrs* d_desc = nullptr;  // the one-entry descriptor array the graph reads
+    uint64_t launches = 0;       // kernels per replay
+};
+
 struct Ctx {
     std::mutex mu;
     bool ready = false;
@@ -224,6 +253,8 @@ struct Ctx {
     PrimeStreams prime_streams = {};
     cudaMemPool_t pool = nullptr;
     bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
+    std::map<GraphKey, GraphEntry> graphs;  // single-product graphs by plan shape
+    cudaStream_t cap = nullptr;             // their capture stream
 };
 
 // 64-bit digits (set 2) for single products: on unless PREC_GPU_WIDE_DIGITS=0;
@@ -346,6 +377,7 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaSetDevice(device));
     c.device = device;
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c.last_done, cudaEventDisableTiming));
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
@@ -453,6 +485,58 @@ static int ensure_io(Ctx& c, size_t limbs) {
 // Enqueues one NTT-band product on device pointers.
 // A square (d_a == d_b, la == lb) transforms its one operand only on the
 // four-step path; the single-CTA path reads the operand twice.
+// One four-step product as a replay of its shape's graph (captured on first
+// use): the descriptor goes up by a stream-ordered copy from host memory
+// that the copy has consumed when it returns, then the graph runs.
+static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStream_t st) {
+    const GraphKey key{pl.set, pl.k, pl.k1, pl.cg, pl.cmr, pl.rmr, pl.rows, args.square};
+    auto it = c.graphs.find(key);
+    if (it == c.graphs.end()) {
+        GraphEntry e;
+        CK(cudaMalloc(&e.d_desc, sizeof(ProdPtrs)));
+        ProdArgs cls = args;  // class-wide fields; the product's own come from the descriptor
+        cls.a = cls.b = nullptr;
+        cls.out = nullptr;
+        cls.work = cls.scratch = nullptr;
+        const uint64_t lout_max = set_wide(pl.set) ? (1ull << pl.k) + 1 : (1ull << pl.k) / 2 + 1;
+        const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+        const int max_nblk = (int)((lout_max + bl - 1) / bl);
+        cudaError_t err = cudaStreamBeginCapture(c.cap, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) {
+            cudaFree(e.d_desc);
+            return cuda_code(err);
+        }
+        const uint64_t before = launches_this_thread();
+        ntt_launch_4step_batch(pl.set, cls, e.d_desc, 1, max_nblk, c.cap);
+        e.launches = launches_this_thread() - before;  // captured, counted at every replay
+        uncount_launches(e.launches);
+        cudaGraph_t g = nullptr;
+        err = cudaStreamEndCapture(c.cap, &g);
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&e.exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (err != cudaSuccess) {
+            cudaFree(e.d_desc);
+            return cuda_code(err);
+        }
+        it = c.graphs.emplace(key, e).first;
+    }
+    ProdPtrs d;
+    d.a = args.a;
+    d.b = args.b;
+    d.out = args.out;
+    d.work = args.work;
+    d.scratch = args.scratch;
+    d.la = args.la;
+    d.lb = args.lb;
+    d.lout = args.lout;
+    d.nblk = args.nblk;
+    d.pad = 0;
+    CK(cudaMemcpyAsync(it->second.d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, st));
+    CK(cudaGraphLaunch(it->second.exec, st));
+    count_launches(it->second.launches);
+    return 0;
+}
+
 static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
                        uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr,
                        cudaEvent_t a_ready = nullptr, cudaEvent_t b_ready = nullptr) {
@@ -494,6 +578,7 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.crt5 = pl.crt5;
         args.f = c.field[pl.set];
         const bool split = c.split_primes && pl.split;
+        if (!split && !ev && pl.k <= kGraphMaxLog2) return enqueue_graph(c, args, pl, st);
         ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready);
     }
     CK(cudaGetLastError());
@@ -766,6 +851,13 @@ void prec_gpu_shutdown(void) {
     }
     cudaEventDestroy(c.prime_streams.fork);
     c.prime_streams = PrimeStreams{};
+    for (auto& kv : c.graphs) {
+        cudaGraphExecDestroy(kv.second.exec);
+        cudaFree(kv.second.d_desc);
+    }
+    c.graphs.clear();
+    cudaStreamDestroy(c.cap);
+    c.cap = nullptr;
     if (c.pool) cudaMemPoolDestroy(c.pool);
     c.pool = nullptr;
     cudaStreamDestroy(c.stream);

@@ -45,11 +45,13 @@ def test_ntt_plan_sizes():
         assert native.ntt_log2(1 << 24, 1 << 24) == 26
         assert native.ntt_log2(1 << 24, (1 << 24) + 1) == 0  # beyond the 2^26-point transform
         native.set_wide_digits(True)
-        # 64-bit digits from 2^13 to 2^22 points, both operands in the lower half
-        assert native.ntt_log2(8192, 8192) == 14
+        # 64-bit digits from 2^18 to 2^25 points, both operands in the lower half
+        assert native.ntt_log2(8192, 8192) == 15
+        assert native.ntt_log2(1 << 16, 1 << 16) == 18
+        assert native.ntt_log2(1 << 17, 1 << 17) == 18
         assert native.ntt_log2(1 << 20, 1 << 20) == 21
         assert native.ntt_log2(1 << 21, 1 << 21) == 22
-        assert native.ntt_log2(3000, 3000) == 13
+        assert native.ntt_log2(3000, 3000) == 14
         assert native.ntt_log2(1 << 20, 1000) == 21
         # one operand above half the 64-bit-digit transform: 32-bit digits
         assert native.ntt_log2(3 << 19, 1 << 19) == 22

@@ -42,7 +42,7 @@ def test_sqr_each_length(gpu):
     """Every transform length 2^5 .. 2^21, both the single-CTA and the
     four-step kernels, squares of operands with the top bit set: 32-bit
     digits (2^k points for 2^(k-2) limbs), then 64-bit digits (2^(k-1)
-    points from 2^13)."""
+    points from 2^18)."""
     for wide in (False, True):
         prev = gpu.set_wide_digits(wide)
         try:
@@ -51,7 +51,7 @@ def test_sqr_each_length(gpu):
                 a = O.splitmix64(k + 500, n)
                 a[-1] |= np.uint64(1 << 63)
                 assert np.array_equal(gpu.mul(a, a, ntt=True), O.mul_ntt(a, a)), (wide, k)
-                assert gpu.last_stats().log2_n == (k - 1 if wide and k >= 14 else k)
+                assert gpu.last_stats().log2_n == (k - 1 if wide and k >= 19 else k)
         finally:
             gpu.set_wide_digits(prev)
 

@@ -38,6 +38,8 @@ def _configs(gpu, k):
 def test_every_config_bit_exact(gpu, k, wide):
     """Every kernel configuration of a length, on 32-bit digits and on 64-bit
     digits (the same kernels on five primes' residues)."""
+    if wide and k < 18:
+        pytest.skip("64-bit digits start at 2^18 points")
     n = 1 << (k - 2)
     if wide:  # both operands within the lower half of 2^k points of 64-bit digits
         shapes = [(2 * n, 2 * n), (2 * n, n + 1)]

@@ -23,17 +23,14 @@ def _mul(gpu, a, b, wide):
 
 # (an, bn, transform log2 with 64-bit digits allowed)
 EDGES = [
-    (2048, 2048, 13),   # 2^12 points would do: below the four-step range, 32-bit digits
-    (2049, 2049, 13),   # the first 64-bit-digit length
-    (4096, 4096, 13),   # both operands exactly half of 2^13 points
-    (4097, 4096, 15),   # one operand above half: 32-bit digits (2^15 points)
-    (4096, 1, 14),      # 4096 + 1 - 1 = 2^12 coefficients: 32-bit digits
-    (4096, 2, 13),      # 4097 coefficients, a at exactly half: 64-bit digits
-    (65536, 65535, 17),
+    (1 << 16, 1 << 16, 18),        # 2^17 coefficients: 2^17 points would be below 2^18, 32-bit digits
+    (1 << 17, 1 << 17, 18),        # the first 64-bit-digit length, both operands exactly half
+    ((1 << 17) + 1, 1 << 17, 20),  # one operand above half: 32-bit digits (2^19 + 2 coefficients)
+    (1 << 17, 1, 19),              # 2^17 coefficients: 32-bit digits
+    (1 << 17, 2, 18),              # 2^17 + 1 coefficients, a at exactly half: 64-bit digits
+    (130000, 100000, 18),
+    (200000, 50001, 19),           # unbalanced: 32-bit digits
     (65537, 65535, 18),
-    (40000, 3, 17),     # unbalanced: 32-bit digits
-    (1 << 16, 1 << 15, 17),
-    (123457, 7001, 18),
 ]
 
 
@@ -49,12 +46,12 @@ def test_edges_vs_oracle(gpu, an, bn, k):
 
 
 def test_random_shapes_both_widths(gpu):
-    """Random shapes 2000 .. 70000 limbs, random and all-ones-heavy
+    """Random shapes 70000 .. 400000 limbs, random and all-ones-heavy
     operands: the two digit widths agree, and agree with the oracle."""
     rng = np.random.default_rng(2024)
-    for t in range(24):
-        an = int(np.exp(rng.uniform(np.log(2000), np.log(70000))))
-        bn = int(np.exp(rng.uniform(np.log(2000), np.log(70000)))) if t % 3 else an
+    for t in range(12):
+        an = int(np.exp(rng.uniform(np.log(70000), np.log(400000))))
+        bn = int(np.exp(rng.uniform(np.log(70000), np.log(400000)))) if t % 3 else an
         a = O.splitmix64(1000 + t, an)
         b = O.splitmix64(2000 + t, bn)
         if t % 4 == 0:

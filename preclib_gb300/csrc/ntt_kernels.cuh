@@ -110,7 +110,7 @@ struct SmallDesc {
 // device error bits
 constexpr int kDevErrTimeout = 1;
 constexpr int kDevErrCarry = 2;
-constexpr int kDevErrPlan = 4;  // a kernel was given a product its plan does not cover
+constexpr int kDevErrPlan = 8;  // a kernel was given a product its plan does not cover
 
 constexpr int kSmallMaxLog2 = 12;
 constexpr int kSmallMinLog2 = 5;

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
     __shared__ uint32_t s_last;
     __shared__ WideEdge s_edge[kCarryThreads / 32];
     const ProdPtrs PP = select_product(args, batch);
-    const uint32_t bid = blockIdx.x;
+    const uint32_t bid = args.crt_blk0 + blockIdx.x;  // chunked CRT: blocks from crt_blk0
     if ((int)bid >= PP.nblk) return;  // batch: a shorter product of the class
     const uint64_t N = 1ull << args.k;
     const int lane = threadIdx.x & 31;
@@ -239,27 +239,35 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
     // ---- phase 2: the last block resolves the carries between blocks.
     // The barrier orders every thread's limb and aggregate stores before
     // thread 0's device-scope fence, which orders them before the counter.
+    // A chunked CRT (one launch per run of blocks, in order on one stream)
+    // joins each chunk on its own: the carry into the chunk comes from the
+    // previous chunk's join, and its carry out goes to the next.
+    const bool chunked = args.chunk_words != nullptr;
+    uint32_t* counter = chunked ? &args.chunk_words[2 * args.crt_chunk] : &PP.scratch[0];
+    const int blo = chunked ? args.crt_blk0 : 0;
+    const int bhi = chunked ? args.crt_blk0 + (int)gridDim.x : PP.nblk;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        s_last = atomicAdd(&PP.scratch[0], 1u) == (uint32_t)PP.nblk - 1 ? 1u : 0u;
+        s_last = atomicAdd(counter, 1u) == (uint32_t)(bhi - blo) - 1 ? 1u : 0u;
     }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    const int nblk = PP.nblk;
-    const int per = (nblk + blockDim.x - 1) / blockDim.x;  // aggregates per thread
-    const int b0 = threadIdx.x * per;
+    const bool cin_chunk = chunked && __ldcg(&args.chunk_words[2 * args.crt_chunk + 1]) != 0;
+    const int nb = bhi - blo;
+    const int per = (nb + blockDim.x - 1) / blockDim.x;  // aggregates per thread
+    const int b0 = blo + threadIdx.x * per, b1 = min(b0 + per, bhi);
     // this thread's run of blocks as one carry element
     bool tG = false, tP = true;
-    for (int b = b0; b < b0 + per && b < nblk; ++b) {
+    for (int b = b0; b < b1; ++b) {
         const uint32_t a = __ldcg(&agg[b]);
         tG = (a & 1u) || (tG && (a & 2u));
         tP = tP && (a & 2u);
     }
-    auto none = [](bool, bool) -> bool { return false; };
-    bool c = block_carry(tG, tP, sh, none);  // carry into this thread's first block
-    for (int b = b0; b < b0 + per && b < nblk; ++b) {
+    auto chunk_in = [&](bool, bool) -> bool { return cin_chunk; };
+    bool c = block_carry(tG, tP, sh, chunk_in);  // carry into this thread's first block
+    for (int b = b0; b < b1; ++b) {
         const uint32_t a = __ldcg(&agg[b]);
         if (c) {
             // the carry enters block b: +1 ripples through its all-ones limbs
@@ -272,12 +280,15 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
         }
         c = (a & 1u) || (c && (a & 2u));
     }
-    // the last block's carry out must be zero: a product fits La+Lb limbs
-    if (b0 < nblk && b0 + per >= nblk && c) atomicOr(args.err, kDevErrCarry);
+    if (b0 < bhi && b1 == bhi) {  // the thread holding the last block
+        if (chunked && !args.crt_last) args.chunk_words[2 * args.crt_chunk + 3] = c ? 1u : 0u;
+        else if (c) atomicOr(args.err, kDevErrCarry);  // a product fits La+Lb limbs
+    }
 }
 
-void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int max_nblk) {
-    const dim3 grid(batch ? max_nblk : a.nblk, 1, count);
+void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int max_nblk,
+                      int nblk_launch) {
+    const dim3 grid(batch ? max_nblk : (nblk_launch > 0 ? nblk_launch : a.nblk), 1, count);
     if (set == 0) k_crt_carry<0><<<grid, kCarryThreads, 0, st>>>(a, batch);
     else if (set == 1) k_crt_carry<1><<<grid, kCarryThreads, 0, st>>>(a, batch);
     else if (set == kWideSet) k_crt_carry<kWideSet><<<grid, kCarryThreads, 0, st>>>(a, batch);
@@ -293,8 +304,20 @@ void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch
     launch_crt_carry(set, args, st, batch, count, max_nblk);
 }
 
+static void launch_crt_chunks(int set, const ProdArgs& args, cudaStream_t st, const CrtChunks& ch) {
+    for (int c = 0; c < ch.count; ++c) {
+        ProdArgs a = args;
+        a.chunk_words = ch.words;
+        a.crt_chunk = c;
+        a.crt_blk0 = ch.blk0[c];
+        a.crt_last = c == ch.count - 1;
+        launch_crt_carry(set, a, st, nullptr, 1, 0, ch.blk0[c + 1] - ch.blk0[c]);
+        cudaEventRecord(ch.done[c], st);
+    }
+}
+
 void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev, const PrimeStreams* ps,
-                      cudaEvent_t a_ready, cudaEvent_t b_ready) {
+                      cudaEvent_t a_ready, cudaEvent_t b_ready, const CrtChunks* chunks) {
     if (ps && !ev) {
         // one chain per prime; the CRT kernel joins them
         const bool staged = a_ready && b_ready && !args.square;
@@ -320,7 +343,8 @@ void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_
             cudaEventRecord(ps->join[p], s);
             cudaStreamWaitEvent(st, ps->join[p], 0);
         }
-        launch_crt_carry(set, args, st);
+        if (chunks) launch_crt_chunks(set, args, st, *chunks);
+        else launch_crt_carry(set, args, st);
         return;
     }
     if (ev) cudaEventRecord(ev[0], st);

@@ -54,7 +54,10 @@ struct ProdArgs {
     int cmr;            // column pass radix cap, 4 or 6 (0: default)
     int operand_only;   // forward columns of one operand: 1 = a, 2 = b (0: both)
     int rmr;            // row pass radix cap, 4 or 6 (0: default)
-    int pad;
+    int crt_chunk;      // CRT in limb chunks (chunk_words set): this launch's chunk
+    int crt_blk0;       //   its first carry block
+    int crt_last;       //   whether it is the last chunk
+    uint32_t* chunk_words;  // per chunk: [2c] finished blocks, [2c+1] carry into chunk c (nullptr: one launch)
     CrtConst crt;       // sets 0 and 1
     Crt5Const crt5;     // set 2
     FieldArgs f;
@@ -146,12 +149,23 @@ struct PrimeStreams {
     cudaEvent_t fork;
     cudaEvent_t join[kMaxPrimes];
 };
+// The CRT of a single product in limb chunks, launched in order: `done[c]`
+// is recorded after chunk c, whose limbs are then final (the caller copies
+// them out while the next chunks run).  `words` (2 * count words) must be
+// zero in stream order before the first chunk.
+constexpr int kCrtMaxChunks = 4;
+struct CrtChunks {
+    int count;
+    int blk0[kCrtMaxChunks + 1];  // chunk c: carry blocks blk0[c] .. blk0[c+1]-1
+    uint32_t* words;
+    cudaEvent_t done[kCrtMaxChunks];
+};
 // With side streams, `a_ready` / `b_ready` (recorded on `st` after each
 // operand's upload) let each prime's forward columns of a start while b is
 // still being copied.
 void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_t* ev = nullptr,
                       const PrimeStreams* ps = nullptr, cudaEvent_t a_ready = nullptr,
-                      cudaEvent_t b_ready = nullptr);
+                      cudaEvent_t b_ready = nullptr, const CrtChunks* chunks = nullptr);
 // the batch form: `count` products of one length class (class-wide fields
 // from `args`, per-product fields from the device array `batch`);
 // max_nblk = the largest carry grid of the class
@@ -170,8 +184,9 @@ void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* ba
                  int nprimes = 0);
 void launch_inv_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
                      int nprimes = 0);
+// (nblk_launch: the blocks of one chunk of a chunked CRT, a.crt_blk0 ..)
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch = nullptr, int count = 1,
-                      int max_nblk = 0);
+                      int max_nblk = 0, int nblk_launch = 0);
 int configure_fwd_cols();
 int configure_inv_cols();
 

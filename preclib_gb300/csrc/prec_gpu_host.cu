@@ -255,6 +255,12 @@ struct Ctx {
     bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
     std::map<GraphKey, GraphEntry> graphs;  // single-product graphs by plan shape
     cudaStream_t cap = nullptr;             // their capture stream
+    // host products with a chunked CRT: each chunk's limbs copy out on
+    // `copy` while the next chunks run
+    cudaStream_t copy = nullptr;
+    cudaEvent_t chunk_done[kCrtMaxChunks] = {};
+    cudaEvent_t copy_done = nullptr;
+    uint32_t* chunk_words = nullptr;  // 2 * kCrtMaxChunks words
 };
 
 // 64-bit digits (set 2) for single products: on unless PREC_GPU_WIDE_DIGITS=0;
@@ -378,6 +384,10 @@ static int init_locked(Ctx& c, int device) {
     c.device = device;
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
+    for (int i = 0; i < kCrtMaxChunks; ++i) CK(cudaEventCreateWithFlags(&c.chunk_done[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c.copy_done, cudaEventDisableTiming));
+    CK(cudaMalloc(&c.chunk_words, 2 * kCrtMaxChunks * sizeof(uint32_t)));
     CK(cudaEventCreateWithFlags(&c.last_done, cudaEventDisableTiming));
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
@@ -539,7 +549,8 @@ static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStrea
 
 static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
                        uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr,
-                       cudaEvent_t a_ready = nullptr, cudaEvent_t b_ready = nullptr) {
+                       cudaEvent_t a_ready = nullptr, cudaEvent_t b_ready = nullptr,
+                       const CrtChunks* chunks = nullptr) {
     const int square = (d_a == d_b && la == lb) ? 1 : 0;
     const uint64_t lout = la + lb;
     if (pl.path == 0) {
@@ -579,7 +590,8 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.f = c.field[pl.set];
         const bool split = c.split_primes && pl.split;
         if (!split && !ev && pl.k <= kGraphMaxLog2) return enqueue_graph(c, args, pl, st);
-        ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready);
+        ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready,
+                         split ? chunks : nullptr);
     }
     CK(cudaGetLastError());
     return 0;
@@ -766,6 +778,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     if (!square) CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(c.ev_b, st));
     CK(cudaEventRecord(c.ev0, st));
+    bool copied = false;  // the result went out chunk by chunk
     if (use_fft) {
         FftArgs f{};
         f.a = d_a;
@@ -790,8 +803,34 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         CK(cudaGetLastError());
     } else if (blocked) {
         if ((r = enqueue_blocked(c, d_a, la, d_b, lb, d_out, st, B))) return r;
-    } else if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st, nullptr, c.ev_a, c.ev_b))) {
-        return r;
+    } else {
+        // a large product's CRT runs in limb chunks; each chunk's limbs copy
+        // out on the copy stream while the next chunks run
+        CrtChunks ch{};
+        const bool chunked = pl.path == 1 && c.split_primes && pl.split && pl.nblk >= 2 * kCrtMaxChunks;
+        if (chunked) {
+            const int per = (pl.nblk + kCrtMaxChunks - 1) / kCrtMaxChunks;
+            ch.count = (pl.nblk + per - 1) / per;  // every chunk nonempty
+            ch.words = c.chunk_words;
+            for (int i = 0; i <= ch.count; ++i) ch.blk0[i] = std::min(i * per, pl.nblk);
+            for (int i = 0; i < ch.count; ++i) ch.done[i] = c.chunk_done[i];
+            CK(cudaMemsetAsync(c.chunk_words, 0, 2 * kCrtMaxChunks * sizeof(uint32_t), st));
+        }
+        if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st, nullptr, c.ev_a, c.ev_b, chunked ? &ch : nullptr)))
+            return r;
+        if (chunked) {
+            const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+            for (int i = 0; i < ch.count; ++i) {
+                const uint64_t lo = std::min((uint64_t)ch.blk0[i] * bl, lout);
+                const uint64_t hi = std::min((uint64_t)ch.blk0[i + 1] * bl, lout);
+                CK(cudaStreamWaitEvent(c.copy, ch.done[i], 0));
+                if (hi > lo)
+                    CK(cudaMemcpyAsync(out + lo, d_out + lo, (hi - lo) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                       c.copy));
+            }
+            CK(cudaEventRecord(c.copy_done, c.copy));
+            copied = true;
+        }
     }
     CK(cudaEventRecord(c.ev1, st));
     // error word and the FFT distance first: a failed product leaves `out` untouched
@@ -799,7 +838,8 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     CK(cudaMemsetAsync(c.d_err, 0, sizeof(int), st));
     if (use_fft) CK(cudaStreamSynchronize(st));
     const bool fft_failed = use_fft && (*c.h_err & kDevErrFftRound);
-    if (!fft_failed) CK(cudaMemcpyAsync(out, d_out, lout * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    if (copied) CK(cudaStreamWaitEvent(st, c.copy_done, 0));
+    else if (!fft_failed) CK(cudaMemcpyAsync(out, d_out, lout * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(c.last_done, st));
     CK(cudaStreamSynchronize(st));
     float ms = 0.f;
@@ -858,6 +898,12 @@ void prec_gpu_shutdown(void) {
     c.graphs.clear();
     cudaStreamDestroy(c.cap);
     c.cap = nullptr;
+    cudaStreamDestroy(c.copy);
+    c.copy = nullptr;
+    for (int i = 0; i < kCrtMaxChunks; ++i) cudaEventDestroy(c.chunk_done[i]);
+    cudaEventDestroy(c.copy_done);
+    cudaFree(c.chunk_words);
+    c.chunk_words = nullptr;
     if (c.pool) cudaMemPoolDestroy(c.pool);
     c.pool = nullptr;
     cudaStreamDestroy(c.stream);

@@ -260,16 +260,16 @@ int prec_gpu_last_stats(prec_gpu_stats_t *st);
  * product runs blocked (an operand above the block size). */
 int prec_gpu_ntt_log2(size_t an, size_t bn);
 
-/* Digits of single NTT-band products (prec_gpu_mul, prec_gpu_sqr,
- * prec_gpu_mul_ntt, prec_gpu_mul_device).  1 (the default; the environment
- * variable PREC_GPU_WIDE_DIGITS=0 starts at 0): a product whose operands
- * both fit in the lower half of a transform of at most 2^22 points takes
- * whole 64-bit limbs as digits over five primes -- half the points of the
- * 32-bit-digit transform -- when that needs fewer butterflies.  0: 32-bit
- * digits over three primes.  The result is the same either way; the batch
- * form and the serving loop always use 32-bit digits.  Returns the previous
- * setting.  No counterpart in the reference, whose mul_ntt always splits
- * limbs into 32-bit digits (src/mul_ntt.cpp:331-342). */
+/* Digits of NTT-band products (prec_gpu_mul, prec_gpu_sqr,
+ * prec_gpu_mul_ntt, prec_gpu_mul_device, the batch form and the serving
+ * loop).  1 (the default; the environment variable PREC_GPU_WIDE_DIGITS=0
+ * starts at 0): a product whose operands both fit in the lower half of a
+ * transform of 2^18 .. 2^25 points takes whole 64-bit limbs as digits over
+ * five primes -- half the points of the 32-bit-digit transform -- when
+ * that needs fewer butterflies.  0: 32-bit digits over three primes.  The
+ * result is the same either way.  Returns the previous setting.  No
+ * counterpart in the reference, whose mul_ntt splits limbs into 16-bit
+ * digits (src/mul_ntt.cpp:331-342). */
 int prec_gpu_set_wide_digits(int on);
 
 /* Block size of blocked products, in limbs (default and maximum 2^24 =

@@ -141,8 +141,8 @@ size_t ntt_small_smem_bytes(int k);
 int ntt_small_threads(int k);
 void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k,
                       const FieldArgs& f, cudaStream_t st, cudaEvent_t* ev = nullptr);
-// Side streams of a single product: the three primes' transform kernels
-// run as independent chains (fork from and join to the caller's stream), so
+// Side streams of a single product: each prime's transform kernels run as
+// an independent chain (fork from and join to the caller's stream), so
 // one prime's tail wave overlaps another prime's work.
 struct PrimeStreams {
     cudaStream_t s[kMaxPrimes];

@@ -308,8 +308,14 @@ __device__ __forceinline__ uint32_t map_compose(uint32_t g, uint32_t f) {
     return r;
 }
 
-constexpr int kFftCarryThreads = 256;
-constexpr int kFftCarryLimbs = 2;  // limbs per thread
+#ifndef PREC_FFT_CARRY_THREADS
+#define PREC_FFT_CARRY_THREADS 256
+#endif
+#ifndef PREC_FFT_CARRY_LIMBS
+#define PREC_FFT_CARRY_LIMBS 2
+#endif
+constexpr int kFftCarryThreads = PREC_FFT_CARRY_THREADS;
+constexpr int kFftCarryLimbs = PREC_FFT_CARRY_LIMBS;  // limbs per thread
 constexpr int kFftCarryBlockLimbs = kFftCarryThreads * kFftCarryLimbs;
 
 // Phase 1 (every block): the block's limbs from the signed coefficient sums,

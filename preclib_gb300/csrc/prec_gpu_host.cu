@@ -589,7 +589,12 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.crt5 = pl.crt5;
         args.f = c.field[pl.set];
         const bool split = c.split_primes && pl.split;
-        if (!split && !ev && pl.k <= kGraphMaxLog2) return enqueue_graph(c, args, pl, st);
+        // (a caller capturing `st` into its own graph gets plain launches: the
+        // descriptor upload reads host memory that is gone at its replay)
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (!split && !ev && pl.k <= kGraphMaxLog2 && cudaStreamIsCapturing(st, &cap) == cudaSuccess &&
+            cap == cudaStreamCaptureStatusNone)
+            return enqueue_graph(c, args, pl, st);
         ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready,
                          split ? chunks : nullptr);
     }

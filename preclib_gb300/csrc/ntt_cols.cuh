@@ -55,7 +55,7 @@ __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __
 }
 
 template <int SET, int M, int C, int MR>
-__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
+__global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M, MR);
     static_assert(NP >= 2, "column transforms have at least two passes");
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256, PREC_COLS_MINB) k_fwd_cols(ProdArgs args,
 }
 
 template <int SET, int M, int C, int MR>
-__global__ void __launch_bounds__(256, PREC_COLS_MINB) k_inv_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
+__global__ void __launch_bounds__(256, cols_minb(M, MR)) k_inv_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M, MR);
     static_assert(NP >= 2, "column transforms have at least two passes");

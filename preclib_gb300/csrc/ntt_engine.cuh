@@ -18,9 +18,18 @@
 #ifndef PREC_ROWS_MINB
 #define PREC_ROWS_MINB 3
 #endif
+// column kernels: 4 CTAs (64 registers) unless a radix-64 pass of a
+// 2^11-point column holds 64 values per thread (3 CTAs, 85 registers: at 64
+// those kernels spill 300-450 bytes)
 #ifndef PREC_COLS_MINB
-#define PREC_COLS_MINB 3
+#define PREC_COLS_MINB 4
 #endif
+#ifndef PREC_COLS_MINB_R64
+#define PREC_COLS_MINB_R64 3
+#endif
+__host__ __device__ constexpr int cols_minb(int m, int mr) {
+    return m >= 11 && mr == 6 ? PREC_COLS_MINB_R64 : PREC_COLS_MINB;
+}
 // unroll factor of the item loops of the shared-memory passes
 #ifndef PREC_PASS_UNROLL
 #define PREC_PASS_UNROLL 1

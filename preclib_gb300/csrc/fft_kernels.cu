@@ -24,6 +24,8 @@
 //                    the max distance exceeds 0.25.
 #include <cuda_runtime.h>
 
+#include <map>
+
 #include "fft_kernels.cuh"
 #include "ntt_kernels.cuh"
 
@@ -155,7 +157,8 @@ __device__ __forceinline__ uint32_t bitrev(uint32_t x, int bits) { return bits ?
 
 // forward column pass: grid N2/C CTAs, C adjacent columns each
 template <int C>
-__global__ void __launch_bounds__(256) k_fft_fwd_cols(FftArgs f) {
+__global__ void __launch_bounds__(256) k_fft_fwd_cols(const FftArgs* __restrict__ fa) {
+    const FftArgs f = *fa;
     extern __shared__ double2 fsm[];
     const int N1 = 1 << f.k1;
     const uint32_t N2 = 1u << f.k2;
@@ -183,7 +186,8 @@ __global__ void __launch_bounds__(256) k_fft_fwd_cols(FftArgs f) {
 
 // row pass: CTA r handles frequency rows k1 = r and N1 - r (one row when
 // they coincide); grid N1/2 + 1
-__global__ void __launch_bounds__(256) k_fft_rows(FftArgs f) {
+__global__ void __launch_bounds__(256) k_fft_rows(const FftArgs* __restrict__ fa) {
+    const FftArgs f = *fa;
     extern __shared__ double2 fsm[];
     const int N1 = 1 << f.k1, N2 = 1 << f.k2;
     const int as = fpad(N2) + 1;
@@ -232,7 +236,8 @@ __global__ void __launch_bounds__(256) k_fft_rows(FftArgs f) {
 
 // inverse column pass, scaling, rounding; grid N2/C
 template <int C>
-__global__ void __launch_bounds__(256) k_fft_inv_cols(FftArgs f) {
+__global__ void __launch_bounds__(256) k_fft_inv_cols(const FftArgs* __restrict__ fa) {
+    const FftArgs f = *fa;
     extern __shared__ double2 fsm[];
     __shared__ double s_max[8];
     const int N1 = 1 << f.k1;
@@ -328,7 +333,8 @@ constexpr int kFftCarryBlockLimbs = kFftCarryThreads * kFftCarryLimbs;
 // and checks that every limb past La+Lb and the final carry are zero.
 // scratch (the transform buffer, free by now): [0] counter, [1 .. nblk]
 // block maps, then the limbs from La+Lb up.
-__global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(FftArgs f) {
+__global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(const FftArgs* __restrict__ fa) {
+    const FftArgs f = *fa;
     __shared__ uint32_t s_wmap[kFftCarryThreads / 32];
     __shared__ uint32_t s_last;
     const double dist = *f.maxdist;
@@ -350,10 +356,13 @@ __global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(FftArgs f) {
     auto limb_ref = [&](int64_t m) -> uint64_t& { return m < Lout ? f.out[m] : high[m - Lout]; };
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // a graph launch uses the largest grid of the transform length: blocks
+    // past this product's limbs only take part in the count below
+    const bool idle = (int)blockIdx.x >= nblk;
     const int64_t m0 = (int64_t)blockIdx.x * kFftCarryBlockLimbs + (int64_t)threadIdx.x * kFftCarryLimbs;
     uint64_t u[kFftCarryLimbs];
     int g[kFftCarryLimbs];
-    {
+    if (!idle) {
         i128 prev = limb_sum_s(f.coef, f.ncoef, f.b, m0 - 1);
 #pragma unroll
         for (int k = 0; k < kFftCarryLimbs; ++k) {
@@ -398,7 +407,7 @@ __global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(FftArgs f) {
             limb_ref(m0 + k) = limb;
         }
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !idle) {
         uint32_t bm = kMapIdentity;
         for (int w = 0; w < kFftCarryThreads / 32; ++w) bm = map_compose(s_wmap[w], bm);
         bmap[blockIdx.x] = bm;
@@ -471,23 +480,67 @@ int fft_configure_kernels() {
     return (int)e;
 }
 
-void fft_launch(const FftArgs& f, cudaStream_t st, cudaEvent_t* ev) {
+static int carry_blocks(uint64_t b, uint64_t ncoef, uint64_t lout) {
+    const int64_t lcoef = (int64_t)((b * ncoef + 63) / 64) + 2;
+    const int64_t L = lcoef > (int64_t)lout ? lcoef : (int64_t)lout;
+    return (int)((L + kFftCarryBlockLimbs - 1) / kFftCarryBlockLimbs);
+}
+
+static void launch4(const FftArgs* d_args, int k1, int k2, int nblk, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], st);
-    const int ncol = (1 << f.k2) / kFftCols;
-    k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
+    const int ncol = (1 << k2) / kFftCols;
+    k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(k1), st>>>(d_args);
     if (ev) cudaEventRecord(ev[1], st);
-    k_fft_rows<<<(1 << f.k1) / 2 + 1, 256, rows_smem(f.k2), st>>>(f);
+    k_fft_rows<<<(1 << k1) / 2 + 1, 256, rows_smem(k2), st>>>(d_args);
     if (ev) cudaEventRecord(ev[2], st);
-    k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f);
+    k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(k1), st>>>(d_args);
     if (ev) cudaEventRecord(ev[3], st);
-    {
-        const int64_t lcoef = (int64_t)(((uint64_t)f.b * f.ncoef + 63) / 64) + 2;
-        const int64_t L = lcoef > (int64_t)f.lout ? lcoef : (int64_t)f.lout;
-        const int nblk = (int)((L + kFftCarryBlockLimbs - 1) / kFftCarryBlockLimbs);
-        k_fft_carry<<<nblk, kFftCarryThreads, 0, st>>>(f);
-    }
+    k_fft_carry<<<nblk, kFftCarryThreads, 0, st>>>(d_args);
     count_launches(4);
     if (ev) cudaEventRecord(ev[4], st);
+}
+
+// One graph per (column, row) length: the four kernels read the product's
+// arguments from the device buffer, and the carry grid is the length's
+// largest (16-bit digits), its extra blocks idle.  Guarded by the caller's
+// library lock.
+static std::map<std::pair<int, int>, cudaGraphExec_t> g_fft_graphs;
+static cudaStream_t g_fft_cap = nullptr;
+
+void fft_release_graphs() {
+    for (auto& kv : g_fft_graphs) cudaGraphExecDestroy(kv.second);
+    g_fft_graphs.clear();
+    if (g_fft_cap) cudaStreamDestroy(g_fft_cap);
+    g_fft_cap = nullptr;
+}
+
+int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev) {
+    cudaError_t e = cudaMemcpyAsync(d_args, &f, sizeof(FftArgs), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return (int)e;
+    if (ev) {
+        launch4(d_args, f.k1, f.k2, carry_blocks(f.b, f.ncoef, f.lout), st, ev);
+        return (int)cudaGetLastError();
+    }
+    const auto key = std::make_pair(f.k1, f.k2);
+    auto it = g_fft_graphs.find(key);
+    if (it == g_fft_graphs.end()) {
+        if (!g_fft_cap && (e = cudaStreamCreateWithFlags(&g_fft_cap, cudaStreamNonBlocking)) != cudaSuccess)
+            return (int)e;
+        if ((e = cudaStreamBeginCapture(g_fft_cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return (int)e;
+        const uint64_t before = launches_this_thread();
+        launch4(d_args, f.k1, f.k2, carry_blocks(16, 1ull << (f.k1 + f.k2), 0), g_fft_cap, nullptr);
+        uncount_launches(launches_this_thread() - before);  // captured: counted at every replay
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(g_fft_cap, &g);
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) return (int)e;
+        it = g_fft_graphs.emplace(key, exec).first;
+    }
+    e = cudaGraphLaunch(it->second, st);
+    if (e == cudaSuccess) count_launches(4);
+    return (int)e;
 }
 
 }  // namespace precgpu

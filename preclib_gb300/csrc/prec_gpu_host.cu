@@ -246,6 +246,7 @@ struct Ctx {
     double* d_maxdist = nullptr;
     double* h_maxdist = nullptr;
     double2* fft_tw = nullptr;  // FP64 band twiddles
+    FftArgs* fft_args = nullptr;  // the FP64 band product's arguments, read by its kernels
     cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // each operand on the device
     cudaEvent_t stage_ev[kMaxStages + 1] = {};
@@ -420,6 +421,7 @@ static int init_locked(Ctx& c, int device) {
     CK((cudaError_t)ntt_configure_kernels());
     CK((cudaError_t)fft_configure_kernels());
     CK(cudaMalloc(&c.fft_tw, fft_table_bytes()));
+    CK(cudaMalloc(&c.fft_args, sizeof(FftArgs)));
     fft_build_table(c.fft_tw, c.stream);
     CK(cudaGetLastError());
     int r = build_tables(c);
@@ -497,7 +499,10 @@ static int ensure_io(Ctx& c, size_t limbs) {
 // four-step path; the single-CTA path reads the operand twice.
 // One four-step product as a replay of its shape's graph (captured on first
 // use): the descriptor goes up by a stream-ordered copy from host memory
-// that the copy has consumed when it returns, then the graph runs.
+// that the copy has consumed when it returns (a small copy from pageable
+// memory travels in the command stream; from page-locked memory it was a
+// DMA read over the host link, 10 us slower per product), then the graph
+// runs.
 static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStream_t st) {
     const GraphKey key{pl.set, pl.k, pl.k1, pl.cg, pl.cmr, pl.rmr, pl.rows, args.square};
     auto it = c.graphs.find(key);
@@ -785,7 +790,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     CK(cudaEventRecord(c.ev0, st));
     bool copied = false;  // the result went out chunk by chunk
     if (use_fft) {
-        FftArgs f{};
+        FftArgs f{};  // pageable: the small upload travels in the command stream
         f.a = d_a;
         f.bp = d_b;
         f.out = d_out;
@@ -804,8 +809,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         f.k = fp.k;
         f.k1 = fp.k1;
         f.k2 = fp.k2;
-        fft_launch(f, st);
-        CK(cudaGetLastError());
+        CK((cudaError_t)fft_launch(f, c.fft_args, st));
     } else if (blocked) {
         if ((r = enqueue_blocked(c, d_a, la, d_b, lb, d_out, st, B))) return r;
     } else {
@@ -882,6 +886,9 @@ void prec_gpu_shutdown(void) {
     cudaFree(c.io);
     cudaFree(c.tables);
     cudaFree(c.fft_tw);
+    cudaFree(c.fft_args);
+    c.fft_args = nullptr;
+    fft_release_graphs();
     cudaFree(c.d_err);
     cudaFreeHost(c.h_err);
     cudaEventDestroy(c.last_done);

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <vector>
 
 #include "fft_kernels.cuh"
 #include "ntt_kernels.cuh"
@@ -157,9 +158,10 @@ __device__ __forceinline__ uint32_t bitrev(uint32_t x, int bits) { return bits ?
 
 // forward column pass: grid N2/C CTAs, C adjacent columns each
 template <int C>
-__global__ void __launch_bounds__(256) k_fft_fwd_cols(const FftArgs* __restrict__ fa) {
-    const FftArgs f = *fa;
+__global__ void __launch_bounds__(256) k_fft_fwd_cols(FftArgs f, FftArgs* publish) {
     extern __shared__ double2 fsm[];
+    // the product's arguments for the three kernels after this one
+    if (blockIdx.x == 0 && threadIdx.x == 0) *publish = f;
     const int N1 = 1 << f.k1;
     const uint32_t N2 = 1u << f.k2;
     const int as = fpad(N1) + 1;
@@ -486,39 +488,51 @@ static int carry_blocks(uint64_t b, uint64_t ncoef, uint64_t lout) {
     return (int)((L + kFftCarryBlockLimbs - 1) / kFftCarryBlockLimbs);
 }
 
-static void launch4(const FftArgs* d_args, int k1, int k2, int nblk, cudaStream_t st, cudaEvent_t* ev) {
+// The first kernel takes the product's arguments by value (launch
+// parameters: no copy in the stream) and stores them at d_args, where the
+// other three read them.
+static void launch4(const FftArgs& f, FftArgs* d_args, int nblk, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], st);
-    const int ncol = (1 << k2) / kFftCols;
-    k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(k1), st>>>(d_args);
+    const int ncol = (1 << f.k2) / kFftCols;
+    k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f, d_args);
     if (ev) cudaEventRecord(ev[1], st);
-    k_fft_rows<<<(1 << k1) / 2 + 1, 256, rows_smem(k2), st>>>(d_args);
+    k_fft_rows<<<(1 << f.k1) / 2 + 1, 256, rows_smem(f.k2), st>>>(d_args);
     if (ev) cudaEventRecord(ev[2], st);
-    k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(k1), st>>>(d_args);
+    k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(d_args);
     if (ev) cudaEventRecord(ev[3], st);
     k_fft_carry<<<nblk, kFftCarryThreads, 0, st>>>(d_args);
     count_launches(4);
     if (ev) cudaEventRecord(ev[4], st);
 }
 
-// One graph per (column, row) length: the four kernels read the product's
-// arguments from the device buffer, and the carry grid is the length's
-// largest (16-bit digits), its extra blocks idle.  Guarded by the caller's
-// library lock.
-static std::map<std::pair<int, int>, cudaGraphExec_t> g_fft_graphs;
+// One graph per (column, row) length, its carry grid the length's largest
+// (16-bit digits; the extra blocks idle).  A replay sets the first node's
+// parameters to the product's arguments.  (An upload of the arguments by
+// a copy in the stream measured 8 us slower per product when the caller's
+// operands were page-locked.)  Guarded by the caller's library lock.
+struct FftGraph {
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t first = nullptr;  // k_fft_fwd_cols
+    cudaKernelNodeParams params{};
+    cudaGraph_t graph = nullptr;  // kept: a node's parameters are set through its graph's node handle
+};
+static std::map<std::pair<int, int>, FftGraph> g_fft_graphs;
 static cudaStream_t g_fft_cap = nullptr;
 
 void fft_release_graphs() {
-    for (auto& kv : g_fft_graphs) cudaGraphExecDestroy(kv.second);
+    for (auto& kv : g_fft_graphs) {
+        cudaGraphExecDestroy(kv.second.exec);
+        cudaGraphDestroy(kv.second.graph);
+    }
     g_fft_graphs.clear();
     if (g_fft_cap) cudaStreamDestroy(g_fft_cap);
     g_fft_cap = nullptr;
 }
 
 int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev) {
-    cudaError_t e = cudaMemcpyAsync(d_args, &f, sizeof(FftArgs), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return (int)e;
+    cudaError_t e;
     if (ev) {
-        launch4(d_args, f.k1, f.k2, carry_blocks(f.b, f.ncoef, f.lout), st, ev);
+        launch4(f, d_args, carry_blocks(f.b, f.ncoef, f.lout), st, ev);
         return (int)cudaGetLastError();
     }
     const auto key = std::make_pair(f.k1, f.k2);
@@ -528,17 +542,43 @@ int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* 
             return (int)e;
         if ((e = cudaStreamBeginCapture(g_fft_cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return (int)e;
         const uint64_t before = launches_this_thread();
-        launch4(d_args, f.k1, f.k2, carry_blocks(16, 1ull << (f.k1 + f.k2), 0), g_fft_cap, nullptr);
+        launch4(f, d_args, carry_blocks(16, 1ull << (f.k1 + f.k2), 0), g_fft_cap, nullptr);
         uncount_launches(launches_this_thread() - before);  // captured: counted at every replay
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(g_fft_cap, &g);
-        cudaGraphExec_t exec = nullptr;
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
-        if (g) cudaGraphDestroy(g);
-        if (e != cudaSuccess) return (int)e;
-        it = g_fft_graphs.emplace(key, exec).first;
+        FftGraph fg;
+        // the forward column node: the one whose kernel is k_fft_fwd_cols
+        size_t n = 0;
+        if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &n);
+        std::vector<cudaGraphNode_t> nodes(n);
+        if (e == cudaSuccess && n) e = cudaGraphGetNodes(g, nodes.data(), &n);
+        for (size_t i = 0; e == cudaSuccess && i < n && !fg.first; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+            cudaKernelNodeParams kp{};
+            if (cudaGraphKernelNodeGetParams(nodes[i], &kp) != cudaSuccess) continue;
+            if (kp.func == (void*)k_fft_fwd_cols<kFftCols>) {
+                fg.first = nodes[i];
+                fg.params = kp;
+            }
+        }
+        if (e == cudaSuccess && !fg.first) e = cudaErrorInvalidValue;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&fg.exec, g, 0);
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return (int)e;
+        }
+        fg.graph = g;
+        it = g_fft_graphs.emplace(key, fg).first;
     }
-    e = cudaGraphLaunch(it->second, st);
+    FftGraph& fg = it->second;
+    FftArgs* pub = d_args;
+    void* params[2] = {const_cast<FftArgs*>(&f), &pub};
+    cudaKernelNodeParams kp = fg.params;
+    kp.kernelParams = params;
+    kp.extra = nullptr;
+    if ((e = cudaGraphExecKernelNodeSetParams(fg.exec, fg.first, &kp)) != cudaSuccess) return (int)e;
+    e = cudaGraphLaunch(fg.exec, st);
     if (e == cudaSuccess) count_launches(4);
     return (int)e;
 }

@@ -33,9 +33,10 @@ constexpr int fpad_host(int i) { return i + (i >> 4); }
 size_t fft_table_bytes();
 void fft_build_table(double2* tw, cudaStream_t st);
 int fft_configure_kernels();
-// The product's 4 kernels: its arguments go up to `d_args` (device) in
-// stream order, then one graph replay (captured once per length), or, with
-// `ev`, plain launches with an event before the first and after each.
+// The product's 4 kernels: the first takes the arguments by value and
+// stores them at `d_args` (device) for the others; one graph replay
+// (captured once per length), or, with `ev`, plain launches with an event
+// before the first and after each.
 // Returns a cudaError_t.  Call with the library lock held.
 int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev = nullptr);
 // destroys the cached graphs (library shutdown)

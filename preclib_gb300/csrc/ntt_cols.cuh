@@ -69,6 +69,8 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs arg
     const uint2* __restrict__ tw = args.f.tf[prime];
     const uint32_t N2 = 1u << args.k2;
     const uint32_t c0 = blockIdx.x * C;
+    // a graph replay's later kernels read the product from `publish`
+    if (args.publish && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *args.publish = P;
 
     // the carry kernel's look-back words start at zero
     if (blockIdx.y == 0 && args.prime0 == 0) {

@@ -36,6 +36,8 @@ struct Crt5Const {
     ShoupC b[10];
 };
 
+struct ProdPtrs;
+
 // One product of the multi-pass (four-step) path.
 struct ProdArgs {
     const uint64_t* a;
@@ -58,6 +60,7 @@ struct ProdArgs {
     int crt_blk0;       //   its first carry block
     int crt_last;       //   whether it is the last chunk
     uint32_t* chunk_words;  // per chunk: [2c] finished blocks, [2c+1] carry into chunk c (nullptr: one launch)
+    ProdPtrs* publish;      // forward columns store the product's ProdPtrs here for the later kernels (or nullptr)
     CrtConst crt;       // sets 0 and 1
     Crt5Const crt5;     // set 2
     FieldArgs f;

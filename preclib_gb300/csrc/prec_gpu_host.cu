@@ -225,8 +225,11 @@ struct GraphKey {
 
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
-    ProdPtrs* d_desc = nullptr;  // the one-entry descriptor array the graph reads
+    ProdPtrs* d_desc = nullptr;  // the one-entry descriptor array the later kernels read
     uint64_t launches = 0;       // kernels per replay
+    cudaGraphNode_t first = nullptr;  // the forward column node: the product's arguments by value
+    cudaKernelNodeParams params{};
+    cudaGraph_t graph = nullptr;  // kept: a node's parameters are set through its graph's node handle
 };
 
 struct Ctx {
@@ -498,17 +501,19 @@ static int ensure_io(Ctx& c, size_t limbs) {
 // A square (d_a == d_b, la == lb) transforms its one operand only on the
 // four-step path; the single-CTA path reads the operand twice.
 // One four-step product as a replay of its shape's graph (captured on first
-// use): the descriptor goes up by a stream-ordered copy from host memory
-// that the copy has consumed when it returns (a small copy from pageable
-// memory travels in the command stream; from page-locked memory it was a
-// DMA read over the host link, 10 us slower per product), then the graph
-// runs.
+// use).  The forward column kernel takes the product by value -- a replay
+// sets that node's parameters -- and stores its descriptor for the row,
+// inverse column and carry kernels, which run in batch form on it.  (An
+// upload of the descriptor by a copy in the stream measured 8-10 us slower
+// per product when the caller's operands were page-locked.)
 static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStream_t st) {
     const GraphKey key{pl.set, pl.k, pl.k1, pl.cg, pl.cmr, pl.rmr, pl.rows, args.square};
     auto it = c.graphs.find(key);
     if (it == c.graphs.end()) {
         GraphEntry e;
         CK(cudaMalloc(&e.d_desc, sizeof(ProdPtrs)));
+        ProdArgs first = args;
+        first.publish = e.d_desc;
         ProdArgs cls = args;  // class-wide fields; the product's own come from the descriptor
         cls.a = cls.b = nullptr;
         cls.out = nullptr;
@@ -522,33 +527,42 @@ static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStrea
             return cuda_code(err);
         }
         const uint64_t before = launches_this_thread();
-        ntt_launch_4step_batch(pl.set, cls, e.d_desc, 1, max_nblk, c.cap);
+        launch_fwd_cols(pl.set, first, c.cap);
+        launch_rows(pl.set, cls, c.cap, e.d_desc, 1);
+        launch_inv_cols(pl.set, cls, c.cap, e.d_desc, 1);
+        launch_crt_carry(pl.set, cls, c.cap, e.d_desc, 1, max_nblk);
         e.launches = launches_this_thread() - before;  // captured, counted at every replay
         uncount_launches(e.launches);
         cudaGraph_t g = nullptr;
         err = cudaStreamEndCapture(c.cap, &g);
+        // the forward column node: the graph's only node without a dependency
+        size_t n = 0;
+        if (err == cudaSuccess) err = cudaGraphGetRootNodes(g, nullptr, &n);
+        cudaGraphNode_t root = nullptr;
+        if (err == cudaSuccess && n == 1) err = cudaGraphGetRootNodes(g, &root, &n);
+        if (err == cudaSuccess && root) err = cudaGraphKernelNodeGetParams(root, &e.params);
+        if (err == cudaSuccess && !root) err = cudaErrorInvalidValue;
+        e.first = root;
         if (err == cudaSuccess) err = cudaGraphInstantiate(&e.exec, g, 0);
-        if (g) cudaGraphDestroy(g);
         if (err != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
             cudaFree(e.d_desc);
             return cuda_code(err);
         }
+        e.graph = g;
         it = c.graphs.emplace(key, e).first;
     }
-    ProdPtrs d;
-    d.a = args.a;
-    d.b = args.b;
-    d.out = args.out;
-    d.work = args.work;
-    d.scratch = args.scratch;
-    d.la = args.la;
-    d.lb = args.lb;
-    d.lout = args.lout;
-    d.nblk = args.nblk;
-    d.pad = 0;
-    CK(cudaMemcpyAsync(it->second.d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, st));
-    CK(cudaGraphLaunch(it->second.exec, st));
-    count_launches(it->second.launches);
+    GraphEntry& e = it->second;
+    ProdArgs first = args;
+    first.publish = e.d_desc;
+    const ProdPtrs* no_batch = nullptr;
+    void* params[2] = {&first, &no_batch};
+    cudaKernelNodeParams kp = e.params;
+    kp.kernelParams = params;
+    kp.extra = nullptr;
+    CK(cudaGraphExecKernelNodeSetParams(e.exec, e.first, &kp));
+    CK(cudaGraphLaunch(e.exec, st));
+    count_launches(e.launches);
     return 0;
 }
 
@@ -905,6 +919,7 @@ void prec_gpu_shutdown(void) {
     c.prime_streams = PrimeStreams{};
     for (auto& kv : c.graphs) {
         cudaGraphExecDestroy(kv.second.exec);
+        cudaGraphDestroy(kv.second.graph);
         cudaFree(kv.second.d_desc);
     }
     c.graphs.clear();

@@ -69,11 +69,11 @@ PI_SOURCES = ("bignum.cpp", "pi_chudnovsky.cpp", "pi_kernels.cu")
 PI_EXE = "pi_gb300"
 
 
-def build_pi() -> str:
+def build_pi(extra=()) -> str:
     """The pi program (pi/*.cpp, host C++) linked against lib/libprecgpu.so."""
     srcs = [os.path.join(PKG, "pi", f) for f in PI_SOURCES]
     out = os.path.join(LIBDIR, PI_EXE)
-    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-pthread",
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-pthread", *extra,
            "-I", os.path.join(PKG, "..", "include"), *srcs, "-L", LIBDIR, "-lprecgpu",
            "-Xlinker", "-rpath=" + LIBDIR, "-o", out + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -79,6 +79,7 @@ struct GpuBackend : MulBackend {
     u64* d_buf = nullptr;  // device copy of the same layout
     size_t d_cap = 0;
     size_t gpu_products = 0, host_products = 0, batches = 0;
+    double mul_seconds = 0.0;  // wall time inside single products (host API)
 
     GpuBackend() { check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream"); }
     ~GpuBackend() override {
@@ -90,6 +91,7 @@ struct GpuBackend : MulBackend {
     static bool small(const Nat& a, const Nat& b) { return std::max(a.size(), b.size()) <= kHostMaxLimbs; }
 
     void mul(const Nat& a, const Nat& b, Nat& out) override {
+        const double t0 = now_sec();
         out.d.assign(a.size() + b.size(), 0);
         if (small(a, b)) {
             mul_school(a.d.data(), a.size(), b.d.data(), b.size(), out.d.data());
@@ -100,6 +102,7 @@ struct GpuBackend : MulBackend {
             ++gpu_products;
         }
         normalize(out);
+        mul_seconds += now_sec() - t0;
     }
 
     void reserve(size_t limbs) {
@@ -685,8 +688,8 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "sqrt_scale %.6f sec\n", ph.sqrt);
         std::fprintf(stderr, "final_div %.6f sec\n", ph.div);
         std::fprintf(stderr, "to_decimal %.6f sec\n", ph.dec);
-        std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu\n", be.gpu_products,
-                     be.host_products, be.batches);
+        std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu single-product time %.3f s\n",
+                     be.gpu_products, be.host_products, be.batches, be.mul_seconds);
     }
     std::fprintf(stderr, "gpu_launches %llu\n",
                  (unsigned long long)(prec_gpu_launch_count() + signed_add_launches()));

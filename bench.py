@@ -48,6 +48,25 @@ WORKLOAD = "1,048,576 x 1,048,576-limb uint64 product (SplitMix64 seeds 3,4)"
 GOLDEN = os.path.join(ROOT, "tests", "golden", "products.json")
 
 
+def host_link(host, devbuf, stream, reps=5):
+    """Pinned host <-> device copy rates in GB/s (median of `reps` copies of
+    `host`'s size each way, CUDA events on `stream`)."""
+    rates = []
+    for dst, src in ((devbuf, host), (host, devbuf)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = []
+        with torch.cuda.stream(stream):
+            for i in range(reps + 2):
+                e0.record(stream)
+                dst.copy_(src, non_blocking=True)
+                e1.record(stream)
+                e1.synchronize()
+                if i >= 2:
+                    ms.append(e0.elapsed_time(e1))
+        rates.append(round(host.numel() * host.element_size() / statistics.median(ms) / 1e6, 1))
+    return rates
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -302,6 +321,7 @@ def run_ours(args):
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
+    link = host_link(ho, to, stream)
 
     # ---- roofline of the dominant kernel (live events) and of the whole product
     peak, peak_kind = _peaks()
@@ -345,6 +365,11 @@ def run_ours(args):
                                  "unit": "GB/s"},
             "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": 8 * (AN + BN),
                     "d2h_bytes_per_step": 8 * (AN + BN)},
+            "host_link": {"h2d_gbs": link[0], "d2h_gbs": link[1],
+                          "transfer_ms": round(8 * (AN + BN) * (1 / link[0] + 1 / link[1]) / 1e6, 4),
+                          "note": "pinned copies of the product's size in each direction (CUDA events); "
+                                  "the e2e copies of both operands in and the product out take transfer_ms "
+                                  "at these rates"},
             "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,

@@ -675,7 +675,7 @@ def run_pi(args):
             ph = {}
             for line in r.stderr.splitlines():
                 parts = line.split()
-                if len(parts) == 3 and parts[2] == "sec":
+                if len(parts) >= 3 and parts[2] == "sec":  # "name seconds sec [(note)]"
                     ph[parts[0]] = float(parts[1])
                 if len(parts) == 2 and parts[0] == "gpu_launches":
                     launches = int(parts[1])

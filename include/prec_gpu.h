@@ -200,7 +200,8 @@ int prec_gpu_batch_create(const prec_gpu_product_t *items, size_t count, prec_gp
 /* Computes every product of the batch on `stream` (asynchronous).  The first
  * call captures the work into a CUDA graph (one stream branch per length
  * class); later calls replay it, recomputing the products from the current
- * contents of the same operand buffers. */
+ * contents of the same operand buffers.  Device-side failures are reported
+ * by prec_gpu_stream_check. */
 int prec_gpu_batch_run(prec_gpu_batch_t *batch, void *stream);
 
 /* Number of length classes and device bytes the batch holds. */
@@ -209,7 +210,8 @@ int prec_gpu_batch_info(const prec_gpu_batch_t *batch, size_t *classes, size_t *
 /* Waits for the device and frees the batch. */
 void prec_gpu_batch_destroy(prec_gpu_batch_t *batch);
 
-/* One-shot batch on `stream`, synchronous (plan, run without a graph, free). */
+/* One-shot batch on `stream`, synchronous (plan, run without a graph, free);
+ * returns the device-side failures too (as prec_gpu_stream_check would). */
 int prec_gpu_mul_batch(const prec_gpu_product_t *items, size_t count, void *stream);
 
 /* ---- serving loop: continuous admission of requests ---------------------

@@ -339,7 +339,8 @@ int prec_gpu_mul_batch(const prec_gpu_product_t* items, size_t count, void* stre
     cudaError_t e = cudaGetLastError();
     batch_free(b);  // the workspace returns to the pool after the batch's work on `st`
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return cuda_code(e);
+    if (e != cudaSuccess) return cuda_code(e);
+    return ctx_take_device_err();  // what the batch's kernels reported
 }
 
 }  // extern "C"

@@ -441,6 +441,23 @@ static int init_locked(Ctx& c, int device) {
 std::mutex& ctx_mutex() { return g_ctx.mu; }
 int ctx_init_locked(int device) { return init_locked(g_ctx, device); }
 const FieldArgs& ctx_field(int set) { return g_ctx.field[set]; }
+
+// The error bits device work has set since the last read, cleared, as a
+// library code (the work must have finished: the caller synchronised).
+static int take_device_err_locked(Ctx& c) {
+    CK(cudaMemcpy(c.h_err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    const int e = *c.h_err;
+    CK(cudaMemset(c.d_err, 0, sizeof(int)));
+    if (e & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
+    if (e) return PREC_GPU_E_INTERNAL;
+    return 0;
+}
+
+int ctx_take_device_err() {
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (!g_ctx.ready) return PREC_GPU_E_NODEV;
+    return take_device_err_locked(g_ctx);
+}
 int* ctx_device_err() { return g_ctx.d_err; }
 cudaMemPool_t ctx_pool() { return g_ctx.pool; }
 
@@ -1018,11 +1035,8 @@ int prec_gpu_stream_check(void* stream) {
     if (!c.ready) return PREC_GPU_E_NODEV;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CK(cudaStreamSynchronize(st));
-    CK(cudaMemcpy(c.h_err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    const int e = *c.h_err;
-    CK(cudaMemset(c.d_err, 0, sizeof(int)));
-    if (e & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
-    if (e) return PREC_GPU_E_INTERNAL;
+    const int r = take_device_err_locked(c);
+    if (r) return r;
     CK(cudaGetLastError());
     return 0;
 }

@@ -81,6 +81,9 @@ std::mutex& ctx_mutex();
 int ctx_init_locked(int device);
 const FieldArgs& ctx_field(int set);
 int* ctx_device_err();
+// reads and clears the device error bits (takes the library lock); 0 or a
+// PREC_GPU_E_* code
+int ctx_take_device_err();
 // the library's stream-ordered memory pool (freed memory stays resident):
 // workspace of one-shot batches
 cudaMemPool_t ctx_pool();

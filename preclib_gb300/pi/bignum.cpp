@@ -396,24 +396,41 @@ static double tnow() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-std::string to_decimal(const Nat& x, size_t width) {
+int decimal_levels(size_t digits) {
+    int J = 0;
+    while ((kLeafDigits << J) < digits) ++J;
+    return J;
+}
+
+DecimalPowers decimal_powers(int levels) {
+    DecimalPowers d;
+    for (int j = 0; j < levels; ++j) {
+        d.pw.push_back(j == 0 ? pow_u64(10, kLeafDigits) : sqr(d.pw[j - 1]));
+        d.P.push_back(bitlen(d.pw[j]) + 2 + 32);
+        d.rx.push_back(recip(d.pw[j], d.P[j]));
+    }
+    return d;
+}
+
+std::string to_decimal(const Nat& x, size_t width, const DecimalPowers* pre) {
     static const bool trace = std::getenv("PI_GB300_TRACE") != nullptr;
     double t0 = tnow();
     // digits of x are at most floor(bitlen * log10(2)) + 1
     const size_t need = std::max<size_t>(width, (size_t)((double)bitlen(x) * 0.30102999566398120) + 2);
-    int J = 0;
-    while ((kLeafDigits << J) < need) ++J;
+    const int J = decimal_levels(need);
     // powers 10^(kLeafDigits * 2^j), j < J, and their reciprocals
-    std::vector<Nat> pw(J > 0 ? J : 0);
-    if (J > 0) pw[0] = pow_u64(10, kLeafDigits);
-    for (int j = 1; j < J; ++j) pw[j] = sqr(pw[j - 1]);
+    DecimalPowers own;
+    if (!pre || (int)pre->pw.size() < J) {
+        own = decimal_powers(J);
+        pre = &own;
+    }
     if (trace) std::fprintf(stderr, "  to_decimal: %d powers %.3f s\n", J, tnow() - t0);
     std::vector<Nat> pieces{x};
     for (int j = J - 1; j >= 0; --j) {
         const double tl = tnow();
-        const Nat& D = pw[j];
-        const size_t nd = bitlen(D), P = nd + 2 + 32;
-        const Nat X = recip(D, P);
+        const Nat& D = pre->pw[j];
+        const size_t nd = bitlen(D), P = pre->P[j];
+        const Nat& X = pre->rx[j];
         const double tr = tnow();
         const size_t m = pieces.size();
         std::vector<Nat> qs(m), rs(m);

@@ -72,8 +72,21 @@ void divmod(const Nat& N, const Nat& D, Nat& q, Nat& r);
 // floor(sqrt(n))
 Nat isqrt(const Nat& n);
 
+// The powers 10^(L * 2^j), j < levels (L = the leaf size in digits), and
+// their reciprocals: all that decimal conversion needs besides x, so a
+// caller that knows the size of x can build them ahead of time.
+struct DecimalPowers {
+    std::vector<Nat> pw;     // 10^(L * 2^j)
+    std::vector<Nat> rx;     // recip(pw[j], bitlen(pw[j]) + 34)
+    std::vector<size_t> P;   // that precision
+};
+// levels the conversion of a number of `digits` decimal digits splits into
+int decimal_levels(size_t digits);
+DecimalPowers decimal_powers(int levels);
+
 // Exact decimal digits of x, padded with leading zeros to at least
-// `width` characters.
-std::string to_decimal(const Nat& x, size_t width);
+// `width` characters; `pre` (optional) holds powers built ahead of time
+// (any number of levels; missing ones are computed here).
+std::string to_decimal(const Nat& x, size_t width, const DecimalPowers* pre = nullptr);
 
 }  // namespace precpi

@@ -14,7 +14,10 @@
 //     (T(a,b) = sum_k t_k P(a,k) Q(k+1,b)), so any tree gives the same Q, T;
 //   * the square root, the final division and the decimal conversion run
 //     Newton iterations whose products go to the GPU (bignum.cpp), the
-//     conversion's splits once more as one batch per level.
+//     conversion's splits once more as one batch per level;
+//   * the square root and the conversion's powers of ten (with their
+//     reciprocals) depend only on the digit count, so a second host thread
+//     computes them while the binary splitting and the division run.
 // The tree's four lowest levels (blocks of 16 terms, products of at most
 // about 20 limbs) and any other product of at most kHostMaxLimbs limbs run
 // on the host threads, as the reference multiplies such sizes with its
@@ -31,7 +34,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <future>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/prec_gpu.h"
@@ -78,8 +84,12 @@ struct GpuBackend : MulBackend {
     size_t h_cap = 0;
     u64* d_buf = nullptr;  // device copy of the same layout
     size_t d_cap = 0;
+    // the square root and the decimal powers run on a second host thread:
+    // single products may come from both threads at once, batches from one
+    // at a time (the staging buffers are shared)
+    std::mutex stats_mu, batch_mu;
     size_t gpu_products = 0, host_products = 0, batches = 0;
-    double mul_seconds = 0.0;  // wall time inside single products (host API)
+    double mul_seconds = 0.0;  // wall time inside single products (host API), summed over threads
 
     GpuBackend() { check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream"); }
     ~GpuBackend() override {
@@ -93,15 +103,16 @@ struct GpuBackend : MulBackend {
     void mul(const Nat& a, const Nat& b, Nat& out) override {
         const double t0 = now_sec();
         out.d.assign(a.size() + b.size(), 0);
-        if (small(a, b)) {
+        const bool host = small(a, b);
+        if (host) {
             mul_school(a.d.data(), a.size(), b.d.data(), b.size(), out.d.data());
-            ++host_products;
         } else {
             const int rc = prec_gpu_mul(a.d.data(), a.size(), b.d.data(), b.size(), out.d.data());
             if (rc) die("prec_gpu_mul", rc);
-            ++gpu_products;
         }
         normalize(out);
+        std::lock_guard<std::mutex> lk(stats_mu);
+        ++(host ? host_products : gpu_products);
         mul_seconds += now_sec() - t0;
     }
 
@@ -122,6 +133,7 @@ struct GpuBackend : MulBackend {
 
     void mul_many(const std::vector<const Nat*>& A, const std::vector<const Nat*>& B,
                   std::vector<Nat>& out) override {
+        std::lock_guard<std::mutex> blk(batch_mu);
         const size_t n = A.size();
         out.assign(n, Nat());
         std::vector<size_t> host, gpu;
@@ -135,7 +147,10 @@ struct GpuBackend : MulBackend {
             mul_school(A[i]->d.data(), A[i]->size(), B[i]->d.data(), B[i]->size(), out[i].d.data());
             normalize(out[i]);
         });
-        host_products += host.size();
+        {
+            std::lock_guard<std::mutex> lk(stats_mu);
+            host_products += host.size();
+        }
         if (gpu.empty()) return;
         // layout: the operands (one copy of an operand repeated within the
         // last few products, e.g. a shared divisor or a node used twice),
@@ -186,6 +201,7 @@ struct GpuBackend : MulBackend {
             out[i].d.assign(h_buf + ooff[u], h_buf + ooff[u] + len);
             normalize(out[i]);
         });
+        std::lock_guard<std::mutex> lk(stats_mu);
         gpu_products += gpu.size();
         ++batches;
     }
@@ -604,12 +620,33 @@ void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
 
 struct Phases {
     double split = 0, sqrt = 0, div = 0, dec = 0;
+    double powers = 0;     // decimal powers and reciprocals (second thread)
+    double root_wait = 0;  // time the main thread waited for the square root
 };
 
 // pi_chudnovsky.cpp:162-194
 std::string pi_digits(size_t digits, Phases& ph) {
     const size_t guard = 10, work = digits + guard, terms = work / 14 + 2;
     double t0 = now_sec();
+    // isqrt(10005 * 10^(2 work)) and the powers of ten of the decimal
+    // conversion do not depend on the series: a second thread computes them
+    // while this one runs the binary splitting and the division (the
+    // reference program computes the same values in sequence)
+    Nat root;
+    DecimalPowers pows;
+    std::promise<void> root_set;
+    std::future<void> root_ready = root_set.get_future();
+    // pi * 10^digits < 4 * 10^digits: at most digits + 1 decimal digits
+    const int levels = decimal_levels(digits + 2);
+    std::thread side([&] {
+        const double s0 = now_sec();
+        root = isqrt(mul_u64(pow_u64(10, 2 * work), 10005));
+        const double s1 = now_sec();
+        root_set.set_value();
+        pows = decimal_powers(levels);
+        ph.sqrt = s1 - s0;
+        ph.powers = now_sec() - s1;
+    });
     Nat Q, T;
     bool tneg = false;
     // PI_GB300_HOST_LEVELS=1: the tree's levels on the host, products staged
@@ -617,18 +654,24 @@ std::string pi_digits(size_t digits, Phases& ph) {
     if (std::getenv("PI_GB300_HOST_LEVELS")) binary_split(terms, Q, T, tneg);
     else binary_split_device(terms, Q, T, tneg);
     double t1 = now_sec();
-    if (tneg || T.zero()) return "error";
-    const Nat n = mul_u64(pow_u64(10, 2 * work), 10005);
-    const Nat root = isqrt(n);
+    root_ready.wait();
     double t2 = now_sec();
+    if (tneg || T.zero()) {
+        side.join();
+        return "error";
+    }
     const Nat num = mul(mul_u64(Q, 426880), root);
     Nat pi, rem;
     divmod(num, T, pi, rem);
     divmod_u64(pi, 10000000000ull);
     double t3 = now_sec();
-    std::string s = to_decimal(pi, 0);
+    side.join();
+    std::string s = to_decimal(pi, 0, &pows);
     double t4 = now_sec();
-    ph = Phases{t1 - t0, t2 - t1, t3 - t2, t4 - t3};
+    ph.split = t1 - t0;
+    ph.root_wait = t2 - t1;
+    ph.div = t3 - t2;
+    ph.dec = t4 - t3;
     if (digits == 0) return s;
     if (s.size() <= digits) s.insert(0, digits + 1 - s.size(), '0');
     s.insert(s.end() - (long long)digits, '.');
@@ -665,11 +708,11 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "pi_gb300: at most 400000000 digits\n");
         return 1;
     }
+    const double t_init = now_sec();
     const int rc = prec_gpu_init(-1);
     if (rc) die("prec_gpu_init", rc);
     GpuBackend be;
     set_backend(&be);
-    now_sec();
     const double start = now_sec();
     Phases ph;
     const std::string out = pi_digits(digits, ph);
@@ -682,10 +725,15 @@ int main(int argc, char** argv) {
         }
         f << out << "\n";
     }
+    const double written = now_sec();
     std::printf("%s\n", short_form(out, full).c_str());
     if (phases) {
+        std::fprintf(stderr, "init %.6f sec\n", start - t_init);
+        std::fprintf(stderr, "write %.6f sec\n", written - start - sec);
         std::fprintf(stderr, "binary_split %.6f sec\n", ph.split);
-        std::fprintf(stderr, "sqrt_scale %.6f sec\n", ph.sqrt);
+        std::fprintf(stderr, "sqrt_scale %.6f sec (second thread)\n", ph.sqrt);
+        std::fprintf(stderr, "decimal_powers %.6f sec (second thread)\n", ph.powers);
+        std::fprintf(stderr, "root_wait %.6f sec\n", ph.root_wait);
         std::fprintf(stderr, "final_div %.6f sec\n", ph.div);
         std::fprintf(stderr, "to_decimal %.6f sec\n", ph.dec);
         std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu single-product time %.3f s\n",

@@ -260,9 +260,20 @@ void divmod(const Nat& N, const Nat& D, Nat& q, Nat& r) {
         r = N;
         return;
     }
+    const size_t P = bitlen(N) - bitlen(D) + 2 + 32;
+    divmod_recip(N, D, recip(D, P), P, q, r);
+}
+
+void divmod_recip(const Nat& N, const Nat& D, const Nat& X, size_t P, Nat& q, Nat& r) {
+    if (D.zero()) fail("division by zero");
+    if (cmp(N, D) < 0) {
+        q = Nat();
+        r = N;
+        return;
+    }
     const size_t nn = bitlen(N), nd = bitlen(D);
-    const size_t P = nn - nd + 2 + 32;
-    const Nat X = recip(D, P);  // ~ 2^(nd + P) / D
+    if (P < nn - nd + 2 + 32) fail("reciprocal precision below the quotient's size");
+    // X ~ 2^(nd + P) / D; N truncated to P + 64 bits
     const size_t s = nn > P + 64 ? nn - (P + 64) : 0;
     q = shr(mul(shr(N, s), X), nd + P - s);
     Nat qd = mul(q, D);

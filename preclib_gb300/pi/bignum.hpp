@@ -69,6 +69,8 @@ Nat pow_u64(u64 base, size_t e);
 Nat recip(const Nat& D, size_t p);
 // exact floor division and remainder (D > 0)
 void divmod(const Nat& N, const Nat& D, Nat& q, Nat& r);
+// the same with X = recip(D, P) computed ahead (P >= bitlen(N) - bitlen(D) + 34)
+void divmod_recip(const Nat& N, const Nat& D, const Nat& X, size_t P, Nat& q, Nat& r);
 // floor(sqrt(n))
 Nat isqrt(const Nat& n);
 

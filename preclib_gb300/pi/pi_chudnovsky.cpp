@@ -23,10 +23,14 @@
 // on the host threads, as the reference multiplies such sizes with its
 // schoolbook and Karatsuba code; everything larger is computed by
 // libprecgpu.  There is no CPU path for those: without a device the
-// program stops.  PI_GB300_TRACE=1 prints the time of every level.
+// program stops.  PI_GB300_TRACE=1 prints the time of every level.  The
+// reported `time` runs from the start of main's work to the finished digits:
+// the library's start-up (on its own thread, beside the tree's bottom blocks
+// on the host threads) is inside it.
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cmath>
 #ifdef __GLIBC__
 #include <malloc.h>
 #endif
@@ -34,7 +38,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <future>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -419,14 +425,25 @@ void small_split(u64 a, u64 b, SmallNode& out) {
     small_signed_add(t1, l.neg, t2, r.neg, out.t, out.neg);
 }
 
-// the bottom level (blocks of `block` terms) computed on the host threads
-// straight into fixed slots of the upload buffer
-void upload_blocks(size_t terms, size_t block, DevLevel& L, cudaStream_t st) {
+// The bottom level (blocks of `block` terms) computed on the host threads
+// straight into fixed slots of the upload buffer; needs no device, so it
+// runs while the device comes up.
+struct HostBlocks {
+    DevLevel L;  // offsets and sizes (no device buffers yet)
+    std::vector<u64> hv;
+    std::vector<int8_t> hs;
+};
+
+HostBlocks host_blocks(size_t terms, size_t block) {
+    HostBlocks B;
+    DevLevel& L = B.L;
+    std::vector<u64>& hv = B.hv;
+    std::vector<int8_t>& hs = B.hs;
     const size_t m = (terms + block - 1) / block;
     constexpr size_t slot = 3 * kSmallLimbs;
     L.op.resize(m), L.oq.resize(m), L.ot.resize(m), L.np.resize(m), L.nq.resize(m), L.nt.resize(m);
-    std::vector<u64> hv(m * slot);
-    std::vector<int8_t> hs(m);
+    hv.resize(m * slot);
+    hs.resize(m);
     parallel_for(m, [&](size_t i) {
         SmallNode nd;
         small_split(i * block, std::min<size_t>(terms, (i + 1) * block), nd);
@@ -438,10 +455,16 @@ void upload_blocks(size_t terms, size_t block, DevLevel& L, cudaStream_t st) {
         L.np[i] = nd.p.n, L.nq[i] = nd.q.n, L.nt[i] = nd.t.n;
         hs[i] = nd.neg ? 1 : 0;
     });
-    L.buf = dev_alloc<u64>(hv.size());
-    L.sign = dev_alloc<int8_t>(m);
-    check_cuda(cudaMemcpyAsync(L.buf, hv.data(), hv.size() * sizeof(u64), cudaMemcpyHostToDevice, st), "level upload");
-    check_cuda(cudaMemcpyAsync(L.sign, hs.data(), m, cudaMemcpyHostToDevice, st), "sign upload");
+    return B;
+}
+
+void upload_blocks(HostBlocks& B, DevLevel& L, cudaStream_t st) {
+    L = std::move(B.L);
+    L.buf = dev_alloc<u64>(B.hv.size());
+    L.sign = dev_alloc<int8_t>(B.hs.size());
+    check_cuda(cudaMemcpyAsync(L.buf, B.hv.data(), B.hv.size() * sizeof(u64), cudaMemcpyHostToDevice, st),
+               "level upload");
+    check_cuda(cudaMemcpyAsync(L.sign, B.hs.data(), B.hs.size(), cudaMemcpyHostToDevice, st), "sign upload");
     check_cuda(cudaStreamSynchronize(st), "level upload");
 }
 
@@ -457,18 +480,19 @@ Nat download(const uint64_t* d, size_t n, cudaStream_t st) {
 bool trace_on();
 Node host_split(u64 a, u64 b);
 
-// Q(0, terms) and T(0, terms): host blocks of 16 terms, then every level on
-// the device (products through one batch per level, T's signed sums by
+constexpr size_t kHostBlock = 16;
+
+// Q(0, terms) and T(0, terms) from the host blocks of 16 terms: every level
+// on the device (products through one batch per level, T's signed sums by
 // signed_add_many); only the root comes back.
-void binary_split_device(size_t terms, Nat& Q, Nat& T, bool& tneg) {
-    constexpr size_t kHostBlock = 16;
+void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
     cudaStream_t st;
     check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
     double t0 = now_sec();
     DevLevel cur;
-    upload_blocks(terms, kHostBlock, cur, st);
-    if (trace_on()) std::fprintf(stderr, "  blocks of %zu terms: %zu nodes on the device %.3f s\n", kHostBlock,
-                                 cur.nodes(), now_sec() - t0);
+    upload_blocks(blocks, cur, st);
+    if (trace_on()) std::fprintf(stderr, "  %zu blocks of %zu terms uploaded %.3f s\n", cur.nodes(), kHostBlock,
+                                 now_sec() - t0);
     std::vector<prec_gpu_product_t> items;
     std::vector<AddPair> pairs;
     std::vector<uint32_t> chunk_pair;
@@ -570,7 +594,6 @@ void binary_split_device(size_t terms, Nat& Q, Nat& T, bool& tneg) {
 void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
     // the lowest levels in blocks of kHostBlock terms on the host threads:
     // their products have at most about 20 limbs
-    constexpr size_t kHostBlock = 16;
     double t0 = now_sec();
     std::vector<Node> lv((terms + kHostBlock - 1) / kHostBlock);
     parallel_for(lv.size(), [&](size_t i) {
@@ -619,14 +642,24 @@ void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
 }
 
 struct Phases {
+    double init = 0;    // the library's start-up (its own thread, beside the host blocks)
+    double blocks = 0;  // the bottom blocks of the tree on the host threads
     double split = 0, sqrt = 0, div = 0, dec = 0;
     double powers = 0;     // decimal powers and reciprocals (second thread)
     double root_wait = 0;  // time the main thread waited for the square root
 };
 
-// pi_chudnovsky.cpp:162-194
-std::string pi_digits(size_t digits, Phases& ph) {
+// pi_chudnovsky.cpp:162-194.  `device_ready` waits for the library's
+// start-up and installs the multiply backend; nothing before it touches the
+// device.
+std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& device_ready) {
     const size_t guard = 10, work = digits + guard, terms = work / 14 + 2;
+    const bool host_levels = std::getenv("PI_GB300_HOST_LEVELS") != nullptr;
+    const double tb = now_sec();
+    HostBlocks blocks;
+    if (!host_levels) blocks = host_blocks(terms, kHostBlock);
+    ph.blocks = now_sec() - tb;
+    device_ready();
     double t0 = now_sec();
     // isqrt(10005 * 10^(2 work)) and the powers of ten of the decimal
     // conversion do not depend on the series: a second thread computes them
@@ -651,26 +684,33 @@ std::string pi_digits(size_t digits, Phases& ph) {
     bool tneg = false;
     // PI_GB300_HOST_LEVELS=1: the tree's levels on the host, products staged
     // through host memory per level (the slower form, for comparison)
-    if (std::getenv("PI_GB300_HOST_LEVELS")) binary_split(terms, Q, T, tneg);
-    else binary_split_device(terms, Q, T, tneg);
+    if (host_levels) binary_split(terms, Q, T, tneg);
+    else binary_split_device(blocks, Q, T, tneg);
     double t1 = now_sec();
-    root_ready.wait();
-    double t2 = now_sec();
     if (tneg || T.zero()) {
         side.join();
         return "error";
     }
-    const Nat num = mul(mul_u64(Q, 426880), root);
+    // T's reciprocal needs no root: its precision comes from a bound on
+    // bitlen(Q * 426880 * root), with bitlen(root) <= log2(sqrt(10005) * 10^work) + 1
+    const Nat q426880 = mul_u64(Q, 426880);
+    const size_t root_bits = (size_t)(std::log2(std::sqrt(10005.0)) + (double)work * std::log2(10.0)) + 2;
+    const size_t P = bitlen(q426880) + root_bits - bitlen(T) + 2 + 32;
+    const Nat X = recip(T, P);
+    const double t2r = now_sec();
+    root_ready.wait();
+    double t2 = now_sec();
+    const Nat num = mul(q426880, root);
     Nat pi, rem;
-    divmod(num, T, pi, rem);
+    divmod_recip(num, T, X, P, pi, rem);
     divmod_u64(pi, 10000000000ull);
     double t3 = now_sec();
     side.join();
     std::string s = to_decimal(pi, 0, &pows);
     double t4 = now_sec();
     ph.split = t1 - t0;
-    ph.root_wait = t2 - t1;
-    ph.div = t3 - t2;
+    ph.root_wait = t2 - t2r;
+    ph.div = (t2r - t1) + (t3 - t2);
     ph.dec = t4 - t3;
     if (digits == 0) return s;
     if (s.size() <= digits) s.insert(0, digits + 1 - s.size(), '0');
@@ -708,14 +748,23 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "pi_gb300: at most 400000000 digits\n");
         return 1;
     }
-    const double t_init = now_sec();
-    const int rc = prec_gpu_init(-1);
-    if (rc) die("prec_gpu_init", rc);
-    GpuBackend be;
-    set_backend(&be);
+    // the device comes up on its own thread while the host threads compute
+    // the bottom blocks of the tree
     const double start = now_sec();
     Phases ph;
-    const std::string out = pi_digits(digits, ph);
+    int init_rc = 0;
+    std::thread init_thread([&] {
+        init_rc = prec_gpu_init(-1);
+        ph.init = now_sec() - start;
+    });
+    std::unique_ptr<GpuBackend> be;
+    auto device_ready = [&] {
+        init_thread.join();
+        if (init_rc) die("prec_gpu_init", init_rc);
+        be.reset(new GpuBackend());
+        set_backend(be.get());
+    };
+    const std::string out = pi_digits(digits, ph, device_ready);
     const double sec = now_sec() - start;
     if (!file.empty()) {
         std::ofstream f(file.c_str(), std::ios::out | std::ios::binary);
@@ -728,7 +777,8 @@ int main(int argc, char** argv) {
     const double written = now_sec();
     std::printf("%s\n", short_form(out, full).c_str());
     if (phases) {
-        std::fprintf(stderr, "init %.6f sec\n", start - t_init);
+        std::fprintf(stderr, "init %.6f sec (its own thread)\n", ph.init);
+        std::fprintf(stderr, "host_blocks %.6f sec\n", ph.blocks);
         std::fprintf(stderr, "write %.6f sec\n", written - start - sec);
         std::fprintf(stderr, "binary_split %.6f sec\n", ph.split);
         std::fprintf(stderr, "sqrt_scale %.6f sec (second thread)\n", ph.sqrt);
@@ -737,7 +787,7 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "final_div %.6f sec\n", ph.div);
         std::fprintf(stderr, "to_decimal %.6f sec\n", ph.dec);
         std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu single-product time %.3f s\n",
-                     be.gpu_products, be.host_products, be.batches, be.mul_seconds);
+                     be->gpu_products, be->host_products, be->batches, be->mul_seconds);
     }
     std::fprintf(stderr, "gpu_launches %llu\n",
                  (unsigned long long)(prec_gpu_launch_count() + signed_add_launches()));

@@ -51,6 +51,7 @@ GOLDEN = os.path.join(ROOT, "tests", "golden", "products.json")
 def host_link(host, devbuf, stream, reps=5):
     """Pinned host <-> device copy rates in GB/s (median of `reps` copies of
     `host`'s size each way, CUDA events on `stream`)."""
+    import torch
     rates = []
     for dst, src in ((devbuf, host), (host, devbuf)):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -19,6 +19,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <new>
+#include <mutex>
 #include <thread>
 
 namespace precpi {
@@ -33,6 +36,50 @@ MulBackend* g_be = nullptr;
 }
 
 }  // namespace
+
+// Free big blocks by capacity.  A block starts with a 64-byte header that
+// holds its capacity; a request takes the smallest free block of at least
+// its size and at most half again as large.
+namespace {
+constexpr size_t kBigHeader = 64;
+constexpr size_t kBigKeep = (size_t)8 << 30;  // free bytes kept at most
+std::mutex g_big_mu;
+std::multimap<size_t, char*> g_big_free;
+size_t g_big_held = 0;
+}  // namespace
+
+void* big_alloc(size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lk(g_big_mu);
+        auto it = g_big_free.lower_bound(bytes);
+        if (it != g_big_free.end() && it->first <= bytes + bytes / 2) {
+            char* b = it->second;
+            g_big_held -= it->first;
+            g_big_free.erase(it);
+            return b + kBigHeader;
+        }
+    }
+    char* b = static_cast<char*>(std::malloc(bytes + kBigHeader));
+    if (!b) throw std::bad_alloc();
+    std::memcpy(b, &bytes, sizeof(bytes));
+    return b + kBigHeader;
+}
+
+void big_free(void* p) noexcept {
+    if (!p) return;
+    char* b = static_cast<char*>(p) - kBigHeader;
+    size_t cap;
+    std::memcpy(&cap, b, sizeof(cap));
+    {
+        std::lock_guard<std::mutex> lk(g_big_mu);
+        if (g_big_held + cap <= kBigKeep) {
+            g_big_free.emplace(cap, b);
+            g_big_held += cap;
+            return;
+        }
+    }
+    std::free(b);
+}
 
 void set_backend(MulBackend* be) { g_be = be; }
 

@@ -11,6 +11,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -19,9 +20,43 @@ namespace precpi {
 using u64 = uint64_t;
 using u128 = unsigned __int128;
 
+// Limb buffers of at least kBigBytes are kept for reuse when freed (up to a
+// bound): the Newton steps and the conversion levels allocate and free
+// numbers of nearly the same sizes over and over, and the C library maps
+// fresh pages for every allocation of that size (a fault and a kernel zero
+// fill per page).  Smaller buffers use the C library's heap.
+constexpr size_t kBigBytes = (size_t)32 << 20;
+void* big_alloc(size_t bytes);
+void big_free(void* p) noexcept;
+
+template <class T>
+struct LimbAlloc {
+    using value_type = T;
+    LimbAlloc() = default;
+    template <class U>
+    LimbAlloc(const LimbAlloc<U>&) noexcept {}
+    T* allocate(size_t n) {
+        if (n * sizeof(T) >= kBigBytes) return static_cast<T*>(big_alloc(n * sizeof(T)));
+        return std::allocator<T>().allocate(n);
+    }
+    void deallocate(T* p, size_t n) noexcept {
+        if (n * sizeof(T) >= kBigBytes) big_free(p);
+        else std::allocator<T>().deallocate(p, n);
+    }
+    template <class U>
+    bool operator==(const LimbAlloc<U>&) const noexcept {
+        return true;
+    }
+    template <class U>
+    bool operator!=(const LimbAlloc<U>&) const noexcept {
+        return false;
+    }
+};
+using Limbs = std::vector<u64, LimbAlloc<u64>>;
+
 // little-endian limbs, no zero top limb (zero = empty)
 struct Nat {
-    std::vector<u64> d;
+    Limbs d;
     Nat() = default;
     explicit Nat(u64 v) {
         if (v) d.push_back(v);

@@ -360,6 +360,7 @@ def run_ours(args):
                          "peak": peak, "unit": "GB/s", "frac": round(dom_gbs / peak, 4),
                          "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes": alg[dom]},
+            "roofline_passes": {k: round(alg[k] / (avg[k] * 1e-3) / 1e9 / peak, 4) for k in avg if k in alg},
             "roofline_product": {"bytes": total_alg,
                                  "achieved": round(total_alg / (per_product_ms * 1e-3 * ws) / 1e9, 1),
                                  "frac": round(total_alg / (per_product_ms * 1e-3 * ws) / 1e9 / peak, 4),

@@ -773,6 +773,11 @@ int main(int argc, char** argv) {
             return 1;
         }
         f << out << "\n";
+        f.flush();
+        if (!f) {
+            std::fprintf(stderr, "pi_gb300: writing %s failed\n", file.c_str());
+            return 1;
+        }
     }
     const double written = now_sec();
     std::printf("%s\n", short_form(out, full).c_str());

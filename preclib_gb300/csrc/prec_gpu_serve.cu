@@ -13,7 +13,10 @@
 //     while others are on the GPU overlap with them; its workspace is
 //     allocated and freed stream-ordered from the pool;
 //   * completion is seen through an event per slot; the latency of a
-//     request is host time from submit() to the observed completion.
+//     request is host time from submit() to the observed completion;
+//   * each slot has its own device error word, copied to pinned host memory
+//     on the slot's stream before the completion event, so a finished
+//     request reports what its kernels flagged.
 // Results do not depend on what else runs: each request has its own
 // workspace, and the kernels are deterministic.
 #include <cuda_runtime.h>
@@ -63,7 +66,8 @@ struct prec_gpu_server {
     size_t budget = 0;
     std::vector<Slot> slots;
     cudaMemPool_t pool = nullptr;
-    int* err = nullptr;  // device error word of the server's kernels
+    int* err = nullptr;    // device error word per slot
+    int* h_err = nullptr;  // its pinned host copy, written before the slot's completion event
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Request> pending;
@@ -85,6 +89,8 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
     const Request& r = sl.req;
     cudaStream_t st = sl.stream;
     const prec_gpu_product_t& p = r.p;
+    const size_t si = (size_t)(&sl - s->slots.data());
+    s->h_err[si] = 0;  // the slot is idle: no copy into it is in flight
     if (p.an == 0 || p.bn == 0) {
         if (p.an + p.bn) cudaMemsetAsync(p.out, 0, (p.an + p.bn) * sizeof(uint64_t), st);
     } else if (r.pl.path == 0) {
@@ -108,7 +114,7 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         args.out = p.out;
         args.work = static_cast<uint32_t*>(ws);
         args.scratch = args.work + ((size_t)2 * r.pl.nprimes << r.pl.k);
-        args.err = s->err;
+        args.err = s->err + si;
         args.la = p.an;
         args.lb = p.bn;
         args.lout = p.an + p.bn;
@@ -125,6 +131,8 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         args.f = ctx_field(r.pl.set);
         ntt_launch_4step(r.pl.set, args, st);
         cudaFreeAsync(ws, st);
+        cudaMemcpyAsync(s->h_err + si, s->err + si, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaMemsetAsync(s->err + si, 0, sizeof(int), st);
     }
     cudaEventRecord(sl.done, st);
     return cuda_code(cudaGetLastError());
@@ -156,7 +164,9 @@ static void worker_loop(prec_gpu_server* s) {
                 if (!sl.busy) continue;
                 const cudaError_t q = cudaEventQuery(sl.done);
                 if (q == cudaErrorNotReady) continue;
-                finish(s, sl, q == cudaSuccess ? PREC_GPU_OK : cuda_code(q));
+                const int e = s->h_err[&sl - s->slots.data()];
+                const int ok = e == 0 ? PREC_GPU_OK : (e & kDevErrTimeout) ? PREC_GPU_E_TIMEOUT : PREC_GPU_E_INTERNAL;
+                finish(s, sl, q == cudaSuccess ? ok : cuda_code(q));
                 s->cv_done.notify_all();
             }
             // admission: FIFO, bounded bypass of a head that does not fit
@@ -232,8 +242,10 @@ int prec_gpu_serve_create(size_t hbm_budget_bytes, int slots, prec_gpu_server_t*
         uint64_t keep = ~0ull;  // keep freed workspace in the pool, resident
         e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
-    if (!e) e = cudaMalloc(&s->err, sizeof(int));
-    if (!e) e = cudaMemset(s->err, 0, sizeof(int));
+    if (!e) e = cudaMalloc(&s->err, slots * sizeof(int));
+    if (!e) e = cudaMemset(s->err, 0, slots * sizeof(int));
+    if (!e) e = cudaMallocHost(&s->h_err, slots * sizeof(int));
+    if (!e) std::fill(s->h_err, s->h_err + slots, 0);
     if (e) {
         prec_gpu_serve_destroy(s);
         return cuda_code(e);
@@ -325,6 +337,7 @@ void prec_gpu_serve_destroy(prec_gpu_server_t* s) {
     }
     if (s->pool) cudaMemPoolDestroy(s->pool);
     if (s->err) cudaFree(s->err);
+    if (s->h_err) cudaFreeHost(s->h_err);
     delete s;
 }
 

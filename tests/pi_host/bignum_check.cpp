@@ -1,4 +1,4 @@
-// bignum_check.cpp -- test driver for the pi program's host arithmetic
+// bignum_check.cpp -- test program for the pi program's host arithmetic
 // (preclib_gb300/pi/bignum.cpp) on a schoolbook multiply backend, so the
 // Newton division, square root and decimal conversion can be checked on a
 // machine without a GPU.  Test infrastructure only: the pi program itself

@@ -1,7 +1,7 @@
 """CPU checks of the pi program's host arithmetic (preclib_gb300/pi/bignum.cpp):
 Newton reciprocal and exact division (with the reciprocal computed at the
 minimum precision and above it), integer square root, and decimal conversion
-(powers built inside or ahead of time), against Python integers.  The driver
+(powers built inside or ahead of time), against Python integers.  The test program
 tests/pi_host/bignum_check.cpp runs the same code on a schoolbook multiply,
 built with 64-digit conversion leaves so that small numbers split over many
 levels."""

@@ -116,6 +116,54 @@ def mod_u64(a, q: int) -> int:
     return int(lib().oracle_mod_u64(_ptr(a), len(a), q))
 
 
+def is_prime_u64(n: int) -> bool:
+    """Miller-Rabin with the first twelve prime bases, deterministic below
+    3.3 * 10^24 (so for every 64-bit n)."""
+    if n < 2:
+        return False
+    bases = (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37)
+    for p in bases:
+        if n % p == 0:
+            return n == p
+    d, s = n - 1, 0
+    while d % 2 == 0:
+        d //= 2
+        s += 1
+    for a in bases:
+        x = pow(a, d, n)
+        if x in (1, n - 1):
+            continue
+        for _ in range(s - 1):
+            x = x * x % n
+            if x == n - 1:
+                break
+        else:
+            return False
+    return True
+
+
+def random_primes61(seed: int, count: int) -> list:
+    """`count` distinct primes in [2^60, 2^61) drawn from a seeded generator:
+    the moduli of the schoolbook spot check (a*b mod q against (a mod q)(b mod q))."""
+    import random
+    rng = random.Random(seed)
+    out = []
+    while len(out) < count:
+        q = rng.randrange(1 << 60, 1 << 61) | 1
+        if q not in out and is_prime_u64(q):
+            out.append(q)
+    return out
+
+
+def spot_check(p, a, b, seed: int, fixed=()) -> None:
+    """Asserts p == a*b modulo the `fixed` moduli and two random 61-bit
+    primes of `seed` (the primes are named in the failure message)."""
+    for q in tuple(fixed) + tuple(random_primes61(seed, 2)):
+        want = mod_u64(a, q) * mod_u64(b, q) % q
+        got = mod_u64(p, q)
+        assert got == want, "product differs modulo %d" % q
+
+
 def splitmix64(seed: int, n: int) -> np.ndarray:
     out = np.zeros(max(n, 1), dtype=np.uint64)
     lib().oracle_splitmix64(seed, n, _ptr(out))

@@ -73,14 +73,13 @@ def test_small_blocks_device_api(gpu):
     assert np.array_equal(to.cpu().numpy().view(np.uint64), O.mul_ntt(a, b))
 
 
-def _spot(p, a, b):
-    for q in (2305843009213693951, 4611686018427387847, 1152921504606846883):
-        assert O.mod_u64(p, q) == O.mod_u64(a, q) * O.mod_u64(b, q) % q
+def _spot(p, a, b, seed=31):
+    O.spot_check(p, a, b, seed, fixed=(2305843009213693951, 4611686018427387847, 1152921504606846883))
 
 
 def test_default_blocks_above_2_24_limbs(gpu):
     """Operands above 2^24 limbs (the reference's mul_fft range): residues
-    modulo three 61/62-bit primes, and the all-ones closed form."""
+    modulo fixed and random 61/62-bit primes, and the all-ones closed form."""
     n = (1 << 24) + 3
     a = O.splitmix64(31, n)
     b = O.splitmix64(32, (1 << 20) + 9)

@@ -114,20 +114,20 @@ def test_torture_ntt(gpu):
             assert np.array_equal(gpu.mul(a, b, ntt=True), O.mul_ntt(a, b)), (p[0], an, bn)
 
 
-def _spot(p, a, b):
-    for q in (2305843009213693951, 4611686018427387847, 1152921504606846883, 2147483647 * 1048573):
-        assert O.mod_u64(p, q) == O.mod_u64(a, q) * O.mod_u64(b, q) % q
+def _spot(p, a, b, seed):
+    O.spot_check(p, a, b, seed, fixed=(2305843009213693951, 4611686018427387847, 1152921504606846883,
+                                       2147483647 * 1048573))
 
 
 def test_large_mod_prime_spot_checks(gpu):
     """Full-size products (2^22 .. 2^26-point transforms): residues modulo
-    61-bit primes agree, plus the top-limb and length invariants."""
+    fixed and random 61-bit primes agree, plus the top-limb and length invariants."""
     for (an, bn, s) in ((1 << 20, 1 << 20, 3), (3 << 20, 1 << 21, 5), (1 << 22, 1 << 22, 7),
                         ((1 << 24) - 5, (1 << 24) - 7, 9)):
         a = O.splitmix64(s, an)
         b = O.splitmix64(s + 1, bn)
         p = gpu.mul(a, b, ntt=True)
-        _spot(p, a, b)
+        _spot(p, a, b, s)
         assert p[-1] != 0 or p[-2] != 0
 
 

@@ -114,3 +114,22 @@ def test_oracle_matches_reference_random():
         ro, re = O.ref_mul_fft(a, b)
         assert np.array_equal(fo, ro) and fe == re
         assert np.array_equal(O.mul(a, b), O.ref_mul(a, b))
+
+
+def test_random_primes61_and_spot_check():
+    """The spot check's moduli are primes in [2^60, 2^61), fixed by the seed,
+    and the check catches a single flipped bit of a product."""
+    qs = O.random_primes61(5, 8)
+    assert qs == O.random_primes61(5, 8) and len(set(qs)) == 8
+    assert all((1 << 60) <= q < (1 << 61) and O.is_prime_u64(q) for q in qs)
+    # composites that fool weaker tests: Carmichael numbers, strong pseudoprimes
+    for n in (561, 1105, 3215031751, 2152302898747, 3474749660383, 341550071728321, 3825123056546413051):
+        assert not O.is_prime_u64(n)
+    assert [n for n in range(2, 60) if O.is_prime_u64(n)] == [2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43,
+                                                              47, 53, 59]
+    a, b = O.splitmix64(1, 300), O.splitmix64(2, 200)
+    p = O.mul_basic(a, b)
+    O.spot_check(p, a, b, 7, fixed=(2305843009213693951,))
+    p[100] ^= np.uint64(1)
+    with pytest.raises(AssertionError):
+        O.spot_check(p, a, b, 7)

@@ -70,10 +70,8 @@ def test_sqr_all_ones(gpu):
         assert np.array_equal(got, want), n
 
 
-def _spot(p, a):
-    for q in (2305843009213693951, 4611686018427387847, 1152921504606846883):
-        r = O.mod_u64(a, q)
-        assert O.mod_u64(p, q) == r * r % q
+def _spot(p, a, seed=3):
+    O.spot_check(p, a, a, seed, fixed=(2305843009213693951, 4611686018427387847, 1152921504606846883))
 
 
 def test_sqr_large_both_prime_sets(gpu):
@@ -88,7 +86,7 @@ def test_sqr_large_both_prime_sets(gpu):
             a = O.splitmix64(s, n)
             p = gpu.sqr(a)
             assert gpu.last_stats().log2_n == k
-            _spot(p, a)
+            _spot(p, a, s)
             assert p[-1] != 0
         finally:
             gpu.set_wide_digits(prev)

@@ -66,8 +66,7 @@ def test_every_config_bit_exact(gpu, k, wide):
 
 
 def _spot(p, a, b):
-    for q in (2305843009213693951, 4611686018427387847):
-        assert O.mod_u64(p, q) == O.mod_u64(a, q) * O.mod_u64(b, q) % q
+    O.spot_check(p, a, b, 91, fixed=(2305843009213693951, 4611686018427387847))
 
 
 @pytest.mark.parametrize("wide", [False, True])

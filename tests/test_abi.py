@@ -114,3 +114,40 @@ def test_noalloc_rejects_oversize():
     sizes alone, before any CUDA call (so this runs without a device)."""
     rc = native.lib().prec_gpu_mul_device_noalloc(1, 65537, 1, 65536, 1, None)
     assert rc == native.E_TOO_LARGE
+
+
+def _fft_bound(b, k):
+    """Error bound of an FP64 convolution of 2^k points on b-bit digits (the
+    library's rule: |x||y| <= N 2^(2b-2), e = 2^-53, beta = 2^-52, doubled
+    for the two operands packed in one complex transform)."""
+    import math
+    e, beta = 2.0 ** -53, 2.0 ** -52
+    g = math.expm1(3 * k * math.log1p(e) + (3 * k + 1) * math.log1p(e * math.sqrt(5)) + 3 * k * math.log1p(beta))
+    return 2.0 * 2.0 ** (k + 2 * b - 2) * g
+
+
+def _fft_width(an, bn):
+    for b in range(16, 7, -1):
+        da, db = (64 * an + b - 1) // b + 1, (64 * bn + b - 1) // b + 1
+        k = 6
+        while (1 << k) < da + db - 1:
+            k += 1
+        if k <= 16 and _fft_bound(b, k) < 0.25:
+            return b
+    return 0
+
+
+def test_fft_digit_width_rule():
+    """The FP64 band takes the widest digit (16 .. 8 bits) whose error bound
+    stays below 1/4 on a transform of at most 2^16 points; outside the band
+    (0 or above 6144 limbs) it reports 0."""
+    import random
+    rng = random.Random(5)
+    shapes = [(1, 1), (193, 193), (1000, 1000), (3000, 3000), (6144, 6144), (6144, 10), (200, 6144),
+              (2048, 2048), (2049, 2039), (4096, 4096)]
+    shapes += [(rng.randrange(1, 6145), rng.randrange(1, 6145)) for _ in range(200)]
+    for an, bn in shapes:
+        assert native.fft_digit_bits(an, bn) == _fft_width(an, bn), (an, bn)
+    assert native.fft_digit_bits(3000, 3000) == 14  # the config-2 FFT product
+    assert native.fft_digit_bits(6145, 6145) == 0
+    assert native.fft_digit_bits(0, 100) == 0

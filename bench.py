@@ -18,6 +18,12 @@ line on rank 0:
          HBM copy bandwidth
   cpu_baseline  the oracle restatement of the reference NTT multiply, one
          thread, a bounded sample of the same product
+  clocks nvidia-smi samples over the timed steps and a sustained window of
+         at least a second of the same step back to back after them
+  config1, fft_3000, batch, serve, pi_1e8  compact results of the other
+         configurations (8192^2 product; 3000^2 on the FP64 band; 4096 uneven
+         products batched vs plain; serving p50/p99; pi to 10^8 digits), each
+         with its own exactness check (--headline-only omits them)
 With --impl reference the same line is produced for the reference's CPU
 algorithm (oracle port; the reference sources do not exist on the GPU
 hosts) run on every host core, one independent product per core.
@@ -46,6 +52,7 @@ SEED_A, SEED_B = 3, 4
 METRIC = "1M×1M-limb mul ms"
 WORKLOAD = "1,048,576 x 1,048,576-limb uint64 product (SplitMix64 seeds 3,4)"
 GOLDEN = os.path.join(ROOT, "tests", "golden", "products.json")
+SUSTAIN_S = 1.2  # seconds of back-to-back steps after the timed ones, for the clock sampler
 
 
 def host_link(host, devbuf, stream, reps=5):
@@ -172,19 +179,25 @@ def dist_env():
     return ws, rank, local
 
 
+def cpu_time(fn, max_products: int, budget_s: float):
+    """Median wall time (ms) of fn() on this host thread over at most
+    `max_products` calls or `budget_s` seconds (at least one call)."""
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < max_products and (not times or time.perf_counter() < t_end):
+        t = time.perf_counter()
+        fn()
+        times.append(time.perf_counter() - t)
+    return statistics.median(times) * 1e3, len(times)
+
+
 def cpu_sample(max_products: int = 3, budget_s: float = 20.0):
     """Oracle restatement of mul_ntt on this host, one thread."""
     import oracle as O
     from preclib_gb300 import workloads
     a = workloads.operand(SEED_A, AN)
     b = workloads.operand(SEED_B, BN)
-    times = []
-    t_end = time.perf_counter() + budget_s
-    while len(times) < max_products and (not times or time.perf_counter() < t_end):
-        t = time.perf_counter()
-        O.mul_ntt(a, b)
-        times.append(time.perf_counter() - t)
-    return statistics.median(times) * 1e3, len(times)
+    return cpu_time(lambda: O.mul_ntt(a, b), max_products, budget_s)
 
 
 def run_reference(args):
@@ -227,6 +240,109 @@ def run_reference(args):
         "e2e": {"value": round(ms, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+CFG1_N, CFG1_SEEDS = 8192, (1, 2)
+
+
+def run_config1(args, flush):
+    """The plain single product of 8192 x 8192 limbs (SplitMix64 seeds 1, 2;
+    NTT band, 2^15 points): device time per product with the operands
+    resident (CUDA events on the launching stream, L2 flushed between
+    steps), the same product end to end through prec_gpu_mul from pinned
+    host buffers, bit-exactness against the reference's mul_ntt output
+    (golden), and the oracle restatement of mul_ntt on one core."""
+    import torch
+
+    import oracle as O
+    from preclib_gb300 import native, workloads
+    dev = flush.device
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    a = workloads.operand(CFG1_SEEDS[0], CFG1_N)
+    b = workloads.operand(CFG1_SEEDS[1], CFG1_N)
+    ta = torch.from_numpy(a.view(np.int64)).to(dev)
+    tb = torch.from_numpy(b.view(np.int64)).to(dev)
+    to = torch.empty(2 * CFG1_N, dtype=torch.int64, device=dev)
+    for _ in range(args.warmup):
+        native.mul_device(ta.data_ptr(), CFG1_N, tb.data_ptr(), CFG1_N, to.data_ptr(), sptr)
+    native.stream_check(sptr)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        evs[i][0].record(stream)
+        native.mul_device(ta.data_ptr(), CFG1_N, tb.data_ptr(), CFG1_N, to.data_ptr(), sptr)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    native.stream_check(sptr)
+    dev_ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in evs)
+    with open(GOLDEN) as f:
+        want = [r for r in json.load(f)["products"] if r["name"] == "cfg1_8192x8192_ntt"][0]["sha256"]
+
+    def sha(x):
+        return hashlib.sha256(np.ascontiguousarray(x, dtype="<u8").tobytes()).hexdigest()
+
+    exact = sha(to.cpu().numpy().view(np.uint64)) == want
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hb = torch.from_numpy(b.view(np.int64)).pin_memory()
+    ho = torch.empty(2 * CFG1_N, dtype=torch.int64).pin_memory()
+    pa, pb, po = (x.numpy().view(np.uint64) for x in (ha, hb, ho))
+    L = native.lib()
+    for _ in range(args.warmup):
+        native.check(L.prec_gpu_mul(native._p(pa), CFG1_N, native._p(pb), CFG1_N, native._p(po)))
+    e2e = []
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        native.check(L.prec_gpu_mul(native._p(pa), CFG1_N, native._p(pb), CFG1_N, native._p(po)))
+        e2e.append(time.perf_counter() - t)
+    plan = native.last_stats()
+    exact = exact and sha(po) == want
+    out = {"workload": "8192 x 8192-limb uint64 product (SplitMix64 seeds 1,2), NTT band",
+           "transform_points": 1 << plan.log2_n, "primes": plan.primes, "digit_bits": plan.digit_bits,
+           "device_ms": round(dev_ms, 4), "e2e_ms": round(statistics.median(e2e) * 1e3, 4),
+           "h2d_bytes_per_step": 16 * CFG1_N, "d2h_bytes_per_step": 16 * CFG1_N,
+           "steps": args.steps, "bit_exact": bool(exact),
+           "l2": "flushed between timed steps (256 MiB write)"}
+    if not args.skip_cpu:
+        cpu_ms, nprod = cpu_time(lambda: O.mul_ntt(a, b), max_products=200, budget_s=2.0)
+        out["cpu_baseline"] = {"value": round(cpu_ms, 4), "unit": "ms", "cores": 1, "kind": "port",
+                               "sample": "%d single-threaded 8192 x 8192 products with the oracle restatement "
+                                         "of mul_ntt (16-bit digits, 2 primes), median" % nprod}
+    return out
+
+
+def sub_results(args, flush):
+    """Compact results of the other benchmark configurations for the default
+    line, each with its own exactness check: the 8192^2 product, the FP64
+    band at 3000^2, the 4096-product batch, the serving loop and pi to 10^8
+    digits (fewer steps than their own workloads take)."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, min(args.steps, 5))
+    sub.warmup = 3
+    res = {"config1": run_config1(args, flush)}
+    f = run_fft(sub, emit=False)
+    res["fft_3000"] = {"device_ms": f["value"], "e2e_ms": f["e2e"]["value"],
+                       "digit_bits": f["config"]["digit_bits"], "transform_points": f["config"]["transform_points"],
+                       "max_rounding_distance": f["max_rounding_distance"],
+                       "reference_max_rounding_distance": f["reference_max_rounding_distance"],
+                       "bit_exact": f["bit_exact"], "cpu_baseline": f.get("cpu_baseline")}
+    bt = run_batch(sub, emit=False)
+    res["batch"] = {"workload": bt["config"]["workload"], "length_classes": bt["config"]["length_classes"],
+                    "batched_products_per_s": bt["value"], "plain_products_per_s": bt["plain_products_per_s"],
+                    "batched_vs_plain": bt["batched_vs_plain"], "device": bt["device"],
+                    "mismatches_vs_plain": bt["mismatches_vs_plain"], "steps": bt["steps"]}
+    sv = run_serve(sub, emit=False)
+    mid = [x for x in sv["loads"] if x["load"] == 0.5][0]
+    res["serve"] = {"workload": sv["config"]["workload"], "capacity_products_per_s": sv["capacity_products_per_s"],
+                    "p50_ms_at_50pct": mid["p50_ms"], "p99_ms_at_50pct": mid["p99_ms"], "loads": sv["loads"],
+                    "mismatches_alone_vs_mixed": sv["mismatches_alone_vs_mixed"], "checked": sv["checked"]}
+    sub.steps = 1
+    pi = run_pi(sub, emit=False)
+    res["pi_1e8"] = {"whole_program_s": pi["value"], "phases_s": pi["phases_s"], "bit_exact": pi["bit_exact"],
+                     "runs": pi["steps"]}
+    return res
 
 
 def run_ours(args):
@@ -274,7 +390,21 @@ def run_ours(args):
             evs[i][1].record(stream)
             flush.fill_(i & 0xFF)
         torch.cuda.synchronize(dev)
-    launches = native.launch_count() - launches0
+        launches = native.launch_count() - launches0
+        # sustained window: the same step back to back for at least a second,
+        # so the clock sampler (200 ms) sees the kernels under load
+        sus = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(64)]
+        sus_ms = []
+        t_sus = time.perf_counter()
+        while time.perf_counter() - t_sus < SUSTAIN_S:
+            for j, (e0, e1) in enumerate(sus):
+                e0.record(stream)
+                step()
+                e1.record(stream)
+                flush.fill_(j & 0xFF)
+            torch.cuda.synchronize(dev)
+            sus_ms.extend(e0.elapsed_time(e1) for e0, e1 in sus)
+        sus_s = time.perf_counter() - t_sus
     clocks = clk.summary()
     native.stream_check(sptr)
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
@@ -340,6 +470,9 @@ def run_ours(args):
         cpu = {"value": round(cpu_ms, 3), "unit": "ms", "cores": 1, "kind": "port",
                "sample": "%d single-threaded 1M x 1M products with the oracle restatement of "
                          "mul_ntt (16-bit digits, 2 primes), median" % nprod}
+    subs = None
+    if rank == 0 and ws == 1 and not args.headline_only:
+        subs = sub_results(args, flush)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(per_product_ms, 4), "unit": "ms", "n_gpus": ws,
@@ -374,8 +507,14 @@ def run_ours(args):
                                   "at these rates"},
             "gpu_launches": launches,
             "clocks": clocks,
+            "clocks_window": "the %d timed steps, then the same step back to back for %.2f s "
+                             "(sustained)" % (args.steps, sus_s),
+            "sustained": {"seconds": round(sus_s, 3), "products": len(sus_ms),
+                          "median_ms": round(statistics.median(sus_ms), 4)},
             "cpu_baseline": cpu,
         }
+        if subs:
+            line.update(subs)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -385,12 +524,13 @@ def run_ours(args):
 BATCH_COUNT, BATCH_SEED = 4096, 7
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     """Batched uneven products: 4096 products, lo log-uniform in [200, 65536]
     limbs, hi = lo * U[1, 2], SplitMix64 operands.  A step is the whole set.
     Batched: one H2D of all operands, one graph replay, one D2H of all
     results.  Plain: prec_gpu_mul per product (host pointers, one call per
-    product).  Both measured end to end, and device-resident."""
+    product).  Both measured end to end, and device-resident.  Returns the
+    line (printed when `emit`)."""
     import torch
 
     from preclib_gb300 import native, workloads
@@ -495,18 +635,21 @@ def run_batch(args):
                 "d2h_bytes_per_step": 8 * o},
         "gpu_launches": launches,
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 SERVE_SEED = 11
 
 
-def run_serve(args):
+def run_serve(args, emit=True):
     """Serving loop: requests with device-resident operands (slices of one
     random device buffer), an = bn = s with s log-uniform in [256, 4194304]
     limbs.  Capacity = products/s with every request queued at once; then
     Poisson arrivals at 10..90 % of capacity, p50/p99 latency per load.
-    A sample of results is recomputed alone and compared with the mix."""
+    A sample of results is recomputed alone and compared with the mix.
+    Returns the line (printed when `emit`)."""
     import hashlib
 
     import torch
@@ -593,20 +736,25 @@ def run_serve(args):
         "mismatches_alone_vs_mixed": int(mismatches), "checked": len(range(0, n_cap, 20)),
         "gpu_launches": native.launch_count() - launches0,
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 FFT_N, FFT_SEEDS = 3000, (5, 6)
 
 
-def run_fft(args):
+def run_fft(args, emit=True):
     """The FP64 FFT band at 3000 x 3000 limbs (SplitMix64 seeds 5, 6): device
     time per product through prec_gpu_mul_fft's kernels (operands resident:
     timed by events around the host call's device part, reported by the
     library), the digit width, the maximum rounding distance of the product,
-    and bit-exactness against the reference's mul_fft output (golden)."""
+    and bit-exactness against the reference's mul_fft output (golden).  The
+    CPU baseline is the oracle restatement of mul_fft on one core, a bounded
+    sample of the same product.  Returns the line (printed when `emit`)."""
     import torch
 
+    import oracle as O
     from preclib_gb300 import native, workloads
     native.init(0)
     a = workloads.operand(FFT_SEEDS[0], FFT_N)
@@ -646,18 +794,26 @@ def run_fft(args):
                 "d2h_bytes_per_step": 16 * FFT_N},
         "gpu_launches": launches, "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    if not args.skip_cpu:
+        cpu_ms, nprod = cpu_time(lambda: O.mul_fft(a, b), max_products=400, budget_s=2.0)
+        line["cpu_baseline"] = {"value": round(cpu_ms, 4), "unit": "ms", "cores": 1, "kind": "port",
+                                "sample": "%d single-threaded 3000 x 3000 products with the oracle restatement "
+                                          "of mul_fft (8-bit digits), median" % nprod}
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 PI_DIGITS = 100000000
 
 
-def run_pi(args):
+def run_pi(args, emit=True):
     """pi to 10^8 decimal digits (the Chudnovsky program, preclib_gb300/pi):
     a step is one whole run of the program (binary splitting with one batch
     per tree level, square root, division, decimal conversion); the output
     file must be byte-identical to preclib's own pi program (SHA-256 of its
-    10^8-digit output, tests/golden/pi.json)."""
+    10^8-digit output, tests/golden/pi.json).  Returns the line (printed
+    when `emit`)."""
     from preclib_gb300 import build as B
     exe = os.path.join(B.LIBDIR, B.PI_EXE)
     with open(os.path.join(ROOT, "tests", "golden", "pi.json")) as f:
@@ -695,7 +851,9 @@ def run_pi(args):
         "e2e": {"value": round(wall, 3), "unit": "s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
         "gpu_launches": launches,
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def ctypes_cast(addr, typ):
@@ -714,6 +872,8 @@ def main():
                          "serve: serving loop under Poisson arrivals; pi: pi to 10^8 digits; "
                          "fft: 3000 x 3000 limbs on the FP64 band")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: omit the other configurations' sub-results")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
     if args.impl == "reference":

@@ -172,9 +172,14 @@ const char *prec_gpu_stage_name(int path, int stage);
  * points); larger products return PREC_GPU_E_TOO_LARGE.  The first call on
  * a device sets that device up (fills the library's twiddle tables with a
  * kernel on `stream` and waits for it), so make the first call before any
- * stream capture.  Calls share the one array: calls that overlap on the
- * GPU (other streams, other threads) race and corrupt each other's result;
- * serialise them.  Asynchronous otherwise; it reports launch errors only. */
+ * stream capture.  A device reset (cudaDeviceReset) discards those tables:
+ * after one, use this entry point only in a new process.  Calls share the
+ * one array: calls that overlap on the GPU (other streams, other threads)
+ * race and corrupt each other's result; serialise them.  Asynchronous
+ * otherwise: the call itself reports size and argument errors (sizes are
+ * checked first, before any CUDA call) and launch errors; an error bit its
+ * kernels raise (an internal fault) stays in a library word until
+ * prec_gpu_stream_check, which reads and clears it without allocating. */
 int prec_gpu_mul_device_noalloc(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,
                                 uint64_t *d_out, void *stream);
 

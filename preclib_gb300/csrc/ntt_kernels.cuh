@@ -175,6 +175,10 @@ void ntt_launch_4step(int set, const ProdArgs& args, cudaStream_t st, cudaEvent_
 void ntt_launch_4step_batch(int set, const ProdArgs& args, const ProdPtrs* batch, int count, int max_nblk,
                             cudaStream_t st);
 int ntt_row_threads(int k2, int n1, int* rows);
+// SMs of the current device (cudaDevAttrMultiProcessorCount, cached per
+// device); GB300's 152 where no device answers (plan queries on a host
+// without a GPU)
+int device_sm_count();
 int ntt_configure_kernels();  // opt-in shared-memory sizes; returns a cudaError_t
 
 // launchers of each translation unit (ntt_cols.cu, ntt_rows.cu, ntt_carry.cu, ntt_small.cu)

@@ -142,7 +142,8 @@ static size_t row_smem(int m, int rows) { return (size_t)rows * 2 * astride_for(
 int ntt_row_threads(int k2, int n1, int* rows_out) {
     int rows = PREC_ROWS_THREADS >> (k2 - 5);
     if (rows < 1) rows = 1;
-    while (rows > 1 && (n1 / rows) * kPrimes < 2 * 152) rows >>= 1;
+    const int sms = device_sm_count();
+    while (rows > 1 && (n1 / rows) * kPrimes < 2 * sms) rows >>= 1;
     int min_rows = k2 >= 10 ? 1 : (1 << (10 - k2));  // >= 32 threads
     if (rows < min_rows) rows = min_rows;
     if (rows > n1) rows = n1;

@@ -72,6 +72,38 @@ static uint32_t neg_inv32(uint32_t m) {  // -m^{-1} mod 2^32 (Newton on 2-adic i
     return 0u - x;
 }
 
+int device_sm_count() {
+    constexpr int kFallbackSms = 152;  // GB300
+    static std::atomic<int> cached[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return kFallbackSms;
+    }
+    int v = cached[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        return kFallbackSms;
+    }
+    cached[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
+const uint32_t* set_primes(int set) { return kP[set]; }
+const uint32_t* set_generators(int set) { return kG[set]; }
+
+PrimeC prime_constants(uint32_t p) {
+    PrimeC pc;
+    pc.p = p;
+    pc.pinv = neg_inv32(p);
+    pc.one_wp = (uint32_t)((1ull << 32) / p);
+    pc.p2 = 2 * p;
+    pc.r32 = (uint32_t)((1ull << 32) % p);
+    pc.r32p = (uint32_t)(((uint64_t)pc.r32 << 32) / p);
+    return pc;
+}
+
 constexpr int kMaxStages = 8;
 
 // kernel names of each path, in launch order
@@ -327,13 +359,7 @@ static int build_tables(Ctx& c) {
         fa.nprimes = kSetPrimes[set];
         for (int j = 0; j < kSetPrimes[set]; ++j) {
             const uint32_t p = kP[set][j];
-            PrimeC& pc = fa.pc[j];
-            pc.p = p;
-            pc.pinv = neg_inv32(p);
-            pc.one_wp = (uint32_t)((1ull << 32) / p);
-            pc.p2 = 2 * p;
-            pc.r32 = (uint32_t)((1ull << 32) % p);
-            pc.r32p = shoup(pc.r32, p).wp;
+            fa.pc[j] = prime_constants(p);
             // g^((p-1)/2) == -1, so wL = g^((p-1)/2^L) has order exactly 2^L
             if (powmod(kG[set][j], (p - 1) / 2, p) != p - 1) return PREC_GPU_E_INTERNAL;
             if (((p - 1) >> L) << L != p - 1) return PREC_GPU_E_INTERNAL;
@@ -1032,11 +1058,16 @@ const char* prec_gpu_stage_name(int path, int stage) {
 int prec_gpu_stream_check(void* stream) {
     Ctx& c = g_ctx;
     std::lock_guard<std::mutex> lk(c.mu);
-    if (!c.ready) return PREC_GPU_E_NODEV;
+    // a caller of the no-allocation entry point alone never starts the
+    // context; its error word is read without allocating anything
+    const bool na = noalloc_ready();
+    if (!c.ready && !na) return PREC_GPU_E_NODEV;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CK(cudaStreamSynchronize(st));
-    const int r = take_device_err_locked(c);
+    const int r = c.ready ? take_device_err_locked(c) : 0;
+    const int rn = na ? noalloc_take_err() : 0;
     if (r) return r;
+    if (rn) return rn;
     CK(cudaGetLastError());
     return 0;
 }

@@ -90,4 +90,16 @@ cudaMemPool_t ctx_pool();
 
 int cuda_code(cudaError_t e);
 
+// the primes and generators of prime set `set` (kSetPrimes[set] entries)
+const uint32_t* set_primes(int set);
+const uint32_t* set_generators(int set);
+// every per-prime constant of PrimeC for the prime p
+PrimeC prime_constants(uint32_t p);
+
+// The no-allocation entry point's device error word on the current device:
+// whether that device has been set up for it, and the word read and
+// cleared (0 or a PREC_GPU_E_* code; the caller has synchronised the work).
+bool noalloc_ready();
+int noalloc_take_err();
+
 }  // namespace precgpu

@@ -17,12 +17,17 @@
 // code those names are host-side stand-ins, not device addresses): the
 // set-up below asks the runtime for each array's device address once per
 // device and passes that address.
+//
+// The device error word g_noalloc_err collects the error bits the kernels
+// raise (a carry out of the product, a plan a kernel does not cover: both
+// mean an internal fault).  prec_gpu_stream_check reads and clears it.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
 #include "../../include/prec_gpu.h"
 #include "ntt_engine.cuh"
+#include "prec_gpu_internal.h"
 
 namespace precgpu {
 
@@ -38,10 +43,12 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWorkWords + 
 static __device__ __align__(256) uint8_t g_noalloc_tables[kTabBytesPerPrime * kPrimes];
 static __device__ __align__(256) int g_noalloc_err;
 
-// prime set 0 (transforms up to 2^23 points; see ntt_field.cuh)
-static const uint32_t kNaP[kPrimes] = {998244353u, 897581057u, 880803841u};
-static const uint32_t kNaG[kPrimes] = {3u, 3u, 26u};
-constexpr int kNaL = 23;
+// prime set 0 (transforms up to 2^23 points; see ntt_field.cuh), the
+// library's own primes and generators (set_primes / set_generators)
+constexpr int kNaSet = 0;
+constexpr int kNaL = kSetMaxLog2[kNaSet];
+// largest product: an + bn limbs (2(an + bn) - 1 digits in 2^18 points)
+constexpr uint64_t kNoAllocMaxLimbs = (uint64_t)1 << (kNoAllocMaxLog2 - 1);
 
 __device__ uint32_t na_powmod(uint32_t b, uint64_t e, uint32_t p) {
     uint64_t r = 1, x = b % p;
@@ -111,6 +118,7 @@ static ShoupC na_shoup(uint32_t w, uint32_t p) { return ShoupC{w, (uint32_t)(((u
 // Garner constants for a 2^k-point transform (the same derivation as the
 // library context's plan).
 static CrtConst na_crt(int k) {
+    const uint32_t* kNaP = set_primes(kNaSet);
     const uint32_t p1 = kNaP[0], p2 = kNaP[1], p3 = kNaP[2];
     uint32_t s[kPrimes];
     for (int j = 0; j < kPrimes; ++j) {
@@ -152,20 +160,22 @@ static int noalloc_setup(int dev, cudaStream_t stream, NoAllocDevice*& out) {
         if (e != cudaSuccess) return na_code(e);
         e = (cudaError_t)ntt_configure_kernels();
         if (e != cudaSuccess) return na_code(e);
-        k_noalloc_tables<<<dim3(kTabEntries / 256, kPrimes), 256, 0, stream>>>(
-            static_cast<uint8_t*>(tables), kNaP[0], kNaP[1], kNaP[2], kNaG[0], kNaG[1], kNaG[2]);
+        const uint32_t* P = set_primes(kNaSet);
+        const uint32_t* G = set_generators(kNaSet);
+        k_noalloc_tables<<<dim3(kTabEntries / 256, kPrimes), 256, 0, stream>>>(static_cast<uint8_t*>(tables), P[0],
+                                                                               P[1], P[2], G[0], G[1], G[2]);
         count_launches(1);
         e = cudaGetLastError();
+        // the error word starts clear (it keeps its bits across calls until
+        // prec_gpu_stream_check reads them)
+        if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) return na_code(e);
         FieldArgs& f = d.field;
         f.max_log2 = kNaL;
         f.nprimes = kPrimes;
         for (int j = 0; j < kPrimes; ++j) {
-            const uint32_t p = kNaP[j];
-            uint32_t inv = 1;
-            for (int i = 0; i < 5; ++i) inv = inv * (2u - p * inv);
-            f.pc[j] = PrimeC{p, 0u - inv, (uint32_t)((1ull << 32) / p), 2 * p};
+            f.pc[j] = prime_constants(P[j]);
             const uint8_t* base = static_cast<const uint8_t*>(tables) + kTabBytesPerPrime * j;
             f.tf[j] = reinterpret_cast<const uint2*>(base);
             f.ti[j] = f.tf[j] + kTabEntries;
@@ -180,17 +190,43 @@ static int noalloc_setup(int dev, cudaStream_t stream, NoAllocDevice*& out) {
     return PREC_GPU_OK;
 }
 
+static NoAllocDevice* current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    return g_noalloc_dev[dev].ready ? &g_noalloc_dev[dev] : nullptr;
+}
+
+bool noalloc_ready() { return current_device() != nullptr; }
+
+int noalloc_take_err() {
+    NoAllocDevice* d = current_device();
+    if (!d) return PREC_GPU_OK;
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, d->err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && h) e = cudaMemset(d->err, 0, sizeof(int));
+    if (e != cudaSuccess) return na_code(e);
+    if (h & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
+    return h ? PREC_GPU_E_INTERNAL : PREC_GPU_OK;
+}
+
 }  // namespace precgpu
 
 using namespace precgpu;
 
 extern "C" int prec_gpu_mul_device_noalloc(const uint64_t* d_a, size_t an, const uint64_t* d_b, size_t bn,
                                            uint64_t* d_out, void* stream) {
+    // sizes first, each bounded before any arithmetic on them (no wrap)
+    if (an > kNoAllocMaxLimbs || bn > kNoAllocMaxLimbs || an + bn > kNoAllocMaxLimbs)
+        return PREC_GPU_E_TOO_LARGE;  // an + bn must not exceed 131072 limbs
     if (!d_a || !d_b || !d_out || an == 0 || bn == 0) return PREC_GPU_E_ARG;
     const uint64_t need = 2 * (uint64_t)an + 2 * (uint64_t)bn - 1;  // digits of the full product
     int k = kSmallMinLog2;
-    while (k <= kNoAllocMaxLog2 && (1ull << k) < need) ++k;
-    if (k > kNoAllocMaxLog2) return PREC_GPU_E_TOO_LARGE;  // an + bn must not exceed 131072 limbs
+    while ((1ull << k) < need) ++k;  // k <= kNoAllocMaxLog2 by the bound above
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return na_code(e);

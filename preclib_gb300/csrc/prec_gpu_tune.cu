@@ -197,7 +197,7 @@ struct Tuner {
         } else {
             int h = 0;
             cudaMemsetAsync(flag, 0, sizeof(int), st);
-            k_tune_diff<<<1216, 256, 0, st>>>(out, ref, 2 * n, flag);
+            k_tune_diff<<<8 * device_sm_count(), 256, 0, st>>>(out, ref, 2 * n, flag);
             count_launches(1);
             cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess || h) return -1.f;
@@ -225,8 +225,8 @@ int tune_one(Tuner& T, int k, KernelConfig& best, float& best_ms, float& default
     int r = plan_for(2 * n, 2 * n, 2 * n, base);
     if (r) return r;
     if (base.path != 1 || base.k != k) return PREC_GPU_E_INTERNAL;
-    k_tune_fill<<<1216, 256, 0, T.st>>>(T.a, n, 0x1234567ull + k);
-    k_tune_fill<<<1216, 256, 0, T.st>>>(T.b, n, 0x7654321ull + k);
+    k_tune_fill<<<8 * device_sm_count(), 256, 0, T.st>>>(T.a, n, 0x1234567ull + k);
+    k_tune_fill<<<8 * device_sm_count(), 256, 0, T.st>>>(T.b, n, 0x7654321ull + k);
     count_launches(2);
     if (cudaGetLastError() != cudaSuccess) return PREC_GPU_E_CUDA;
     best = default_config(k);

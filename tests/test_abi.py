@@ -111,9 +111,15 @@ def test_block_limbs():
 
 def test_noalloc_rejects_oversize():
     """The no-allocation entry point refuses more than 131072 limbs from the
-    sizes alone, before any CUDA call (so this runs without a device)."""
-    rc = native.lib().prec_gpu_mul_device_noalloc(1, 65537, 1, 65536, 1, None)
-    assert rc == native.E_TOO_LARGE
+    sizes alone, before any CUDA call and before it looks at the pointers
+    (so this runs without a device, with null pointers).  Sizes whose sum
+    or doubled sum wraps 64 bits are refused the same way."""
+    L = native.lib()
+    for an, bn in ((65537, 65536), (1 << 63, 1), (1, 1 << 63), ((1 << 64) - 1, 2), (131072, 1), (131073, 0)):
+        assert L.prec_gpu_mul_device_noalloc(None, an, None, bn, None, None) == native.E_TOO_LARGE, (an, bn)
+    # within the limit, the null pointers are the error
+    assert L.prec_gpu_mul_device_noalloc(None, 65536, None, 65536, None, None) == native.E_ARG
+    assert L.prec_gpu_mul_device_noalloc(None, 0, None, 0, None, None) == native.E_ARG
 
 
 def _fft_bound(b, k):

@@ -251,8 +251,14 @@ def test_invalid_arguments(gpu):
     assert L.prec_gpu_mul(null, 8, gpu._p(a), 8, gpu._p(out)) == gpu.E_ARG
     assert L.prec_gpu_mul(gpu._p(a), 8, gpu._p(a), 8, null) == gpu.E_ARG
     assert L.prec_gpu_sqr(null, 3, gpu._p(out)) == gpu.E_ARG
-    assert L.prec_gpu_mul_device(None, 5, 1, 5, 1, None) == gpu.E_ARG
-    assert L.prec_gpu_mul_device(1, 0, 1, 5, 1, None) == gpu.E_ARG
+    # real device buffers beside the invalid argument: were a refusal ever
+    # to move, no kernel is handed an address that is not device memory
+    torch = pytest.importorskip("torch")
+    da = torch.zeros(5, dtype=torch.int64, device="cuda")
+    db = torch.zeros(5, dtype=torch.int64, device="cuda")
+    dout = torch.zeros(10, dtype=torch.int64, device="cuda")
+    assert L.prec_gpu_mul_device(None, 5, db.data_ptr(), 5, dout.data_ptr(), None) == gpu.E_ARG
+    assert L.prec_gpu_mul_device(da.data_ptr(), 0, db.data_ptr(), 5, dout.data_ptr(), None) == gpu.E_ARG
     assert gpu.launch_count() == c0
     # zero-length operands are a valid zero product
     assert L.prec_gpu_mul(null, 0, gpu._p(a), 8, gpu._p(out)) == gpu.OK

@@ -75,8 +75,15 @@ def test_mixed_equals_alone(gpu):
 
 
 def test_oversize_request_refused(gpu):
+    torch = pytest.importorskip("torch")
     srv = gpu.Server(hbm_budget_bytes=1 << 20, slots=2)
+    # real device buffers: the refusal is the host's, but no kernel could
+    # ever be handed an address that is not device memory
+    da = torch.zeros(1 << 20, dtype=torch.int64, device="cuda")
+    db = torch.zeros(1 << 20, dtype=torch.int64, device="cuda")
+    dout = torch.zeros(2 << 20, dtype=torch.int64, device="cuda")
     with pytest.raises(gpu.PrecGpuError) as e:
-        srv.submit(1, 1 << 20, 1, 1 << 20, 1)  # needs ~100 MB of workspace; refused on the host
+        # needs ~100 MB of workspace; refused on the host
+        srv.submit(da.data_ptr(), 1 << 20, db.data_ptr(), 1 << 20, dout.data_ptr())
     assert e.value.code == gpu.E_NOMEM
     srv.close()

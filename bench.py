@@ -299,11 +299,32 @@ def run_config1(args, flush):
         e2e.append(time.perf_counter() - t)
     plan = native.last_stats()
     exact = exact and sha(po) == want
+    # host calls from 1 and from 4 threads (each thread its own stream and
+    # workspace; ctypes releases the interpreter lock during a call)
+    from concurrent.futures import ThreadPoolExecutor
+    per = 200
+    outs = [np.empty(2 * CFG1_N, np.uint64) for _ in range(4)]
+
+    def worker(t):
+        o = outs[t]
+        for _ in range(per):
+            native.check(L.prec_gpu_mul(native._p(pa), CFG1_N, native._p(pb), CFG1_N, native._p(o)))
+        return sha(o) == want
+
+    threads = {}
+    for nt in (1, 4):
+        with ThreadPoolExecutor(nt) as ex:
+            list(ex.map(worker, range(nt)))  # warm-up: each thread's lane
+            t = time.perf_counter()
+            ok = all(ex.map(worker, range(nt)))
+            threads[str(nt)] = round(nt * per / (time.perf_counter() - t), 1)
+        exact = exact and ok
     out = {"workload": "8192 x 8192-limb uint64 product (SplitMix64 seeds 1,2), NTT band",
            "transform_points": 1 << plan.log2_n, "primes": plan.primes, "digit_bits": plan.digit_bits,
            "device_ms": round(dev_ms, 4), "e2e_ms": round(statistics.median(e2e) * 1e3, 4),
            "h2d_bytes_per_step": 16 * CFG1_N, "d2h_bytes_per_step": 16 * CFG1_N,
            "steps": args.steps, "bit_exact": bool(exact),
+           "host_calls_products_per_s_by_threads": threads,
            "l2": "flushed between timed steps (256 MiB write)"}
     if not args.skip_cpu:
         cpu_ms, nprod = cpu_time(lambda: O.mul_ntt(a, b), max_products=200, budget_s=2.0)

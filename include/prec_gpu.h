@@ -56,7 +56,8 @@ typedef struct prec_gpu_stats {
  * src/mul_ntt.cpp:182-191, and a static FFT plan cache, src/mul_fft.cpp:78-100). */
 int prec_gpu_init(int device);
 
-/* Releases every device resource of the library. */
+/* Releases every device resource of the library.  Call it only when no
+ * other thread is inside the library. */
 void prec_gpu_shutdown(void);
 
 /* Full product of two host limb vectors, out[0 .. an+bn) written.
@@ -64,7 +65,11 @@ void prec_gpu_shutdown(void);
  * (replaces mul_fft, src/mul_fft.cpp:386-394), larger -> NTT band
  * (replaces mul_ntt, src/mul_ntt.cpp:494-518).  Squares above 6144 limbs
  * and products of any size below 193 limbs also run on the GPU.
- * Thread-safe (calls are serialised on one device context). */
+ * Thread-safe: each calling thread has its own stream, workspace and
+ * staging buffers (up to 16 threads; more share them round-robin), so
+ * products called from different threads run concurrently on the device,
+ * as the reference's per-thread NTT plans let its threads multiply in
+ * parallel (src/mul_ntt.cpp:182-191). */
 int prec_gpu_mul(const uint64_t *a, size_t an, const uint64_t *b, size_t bn, uint64_t *out);
 
 /* NTT band forced, host pointers (replaces mul_ntt, src/mul_ntt.cpp:494). */
@@ -142,8 +147,10 @@ int prec_gpu_fft_digit_bits(size_t an, size_t bn);
  * NULL = legacy default stream) without host synchronisation.  Operands
  * stay as given (no trimming of zero high limbs).  The call returns after
  * enqueueing; device-side failures (bounded waits) are reported by
- * prec_gpu_stream_check.  Successive calls share the library's workspace
- * and are ordered after one another even across streams.  d_out must not
+ * prec_gpu_stream_check.  Successive calls from one thread share that
+ * thread's workspace and are ordered after one another even across
+ * streams; calls from different threads use separate workspaces and may
+ * run concurrently.  d_out must not
  * overlap the operands.  Operands above the block size run blocked (see
  * prec_gpu_set_block_limbs). */
 int prec_gpu_mul_device(const uint64_t *d_a, size_t an, const uint64_t *d_b, size_t bn,

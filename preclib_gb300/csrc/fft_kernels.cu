@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "fft_kernels.cuh"
@@ -505,47 +507,55 @@ static void launch4(const FftArgs& f, FftArgs* d_args, int nblk, cudaStream_t st
     if (ev) cudaEventRecord(ev[4], st);
 }
 
-// One graph per (column, row) length, its carry grid the length's largest
-// (16-bit digits; the extra blocks idle).  A replay sets the first node's
-// parameters to the product's arguments.  (An upload of the arguments by
-// a copy in the stream measured 8 us slower per product when the caller's
-// operands were page-locked.)  Guarded by the caller's library lock.
+// One graph per (column, row) length and argument buffer (each library
+// lane has its own), its carry grid the length's largest (16-bit digits;
+// the extra blocks idle).  A replay sets the first node's parameters to
+// the product's arguments.  (An upload of the arguments by a copy in the
+// stream measured 8 us slower per product when the caller's operands were
+// page-locked.)  The map is shared by the lanes (g_fft_mu); a graph is
+// only replayed by its own lane, one product at a time.
 struct FftGraph {
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t first = nullptr;  // k_fft_fwd_cols
     cudaKernelNodeParams params{};
     cudaGraph_t graph = nullptr;  // kept: a node's parameters are set through its graph's node handle
 };
-static std::map<std::pair<int, int>, FftGraph> g_fft_graphs;
-static cudaStream_t g_fft_cap = nullptr;
+typedef std::tuple<int, int, const FftArgs*> FftGraphKey;
+static std::map<FftGraphKey, FftGraph> g_fft_graphs;
+static std::mutex g_fft_mu;
 
-void fft_release_graphs() {
-    for (auto& kv : g_fft_graphs) {
-        cudaGraphExecDestroy(kv.second.exec);
-        cudaGraphDestroy(kv.second.graph);
+void fft_release_graphs(const FftArgs* d_args) {
+    std::lock_guard<std::mutex> lk(g_fft_mu);
+    for (auto it = g_fft_graphs.begin(); it != g_fft_graphs.end();) {
+        if (d_args && std::get<2>(it->first) != d_args) {
+            ++it;
+            continue;
+        }
+        cudaGraphExecDestroy(it->second.exec);
+        cudaGraphDestroy(it->second.graph);
+        it = g_fft_graphs.erase(it);
     }
-    g_fft_graphs.clear();
-    if (g_fft_cap) cudaStreamDestroy(g_fft_cap);
-    g_fft_cap = nullptr;
 }
 
-int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev) {
+int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev, cudaStream_t cap) {
     cudaError_t e;
-    if (ev) {
+    if (ev || !cap) {
         launch4(f, d_args, carry_blocks(f.b, f.ncoef, f.lout), st, ev);
         return (int)cudaGetLastError();
     }
-    const auto key = std::make_pair(f.k1, f.k2);
-    auto it = g_fft_graphs.find(key);
+    const FftGraphKey key(f.k1, f.k2, d_args);
+    std::map<FftGraphKey, FftGraph>::iterator it;
+    {
+        std::lock_guard<std::mutex> lk(g_fft_mu);
+        it = g_fft_graphs.find(key);
+    }
     if (it == g_fft_graphs.end()) {
-        if (!g_fft_cap && (e = cudaStreamCreateWithFlags(&g_fft_cap, cudaStreamNonBlocking)) != cudaSuccess)
-            return (int)e;
-        if ((e = cudaStreamBeginCapture(g_fft_cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return (int)e;
+        if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return (int)e;
         const uint64_t before = launches_this_thread();
-        launch4(f, d_args, carry_blocks(16, 1ull << (f.k1 + f.k2), 0), g_fft_cap, nullptr);
+        launch4(f, d_args, carry_blocks(16, 1ull << (f.k1 + f.k2), 0), cap, nullptr);
         uncount_launches(launches_this_thread() - before);  // captured: counted at every replay
         cudaGraph_t g = nullptr;
-        e = cudaStreamEndCapture(g_fft_cap, &g);
+        e = cudaStreamEndCapture(cap, &g);
         FftGraph fg;
         // the forward column node: the one whose kernel is k_fft_fwd_cols
         size_t n = 0;
@@ -569,6 +579,7 @@ int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* 
             return (int)e;
         }
         fg.graph = g;
+        std::lock_guard<std::mutex> lk(g_fft_mu);
         it = g_fft_graphs.emplace(key, fg).first;
     }
     FftGraph& fg = it->second;

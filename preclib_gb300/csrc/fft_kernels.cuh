@@ -35,11 +35,13 @@ void fft_build_table(double2* tw, cudaStream_t st);
 int fft_configure_kernels();
 // The product's 4 kernels: the first takes the arguments by value and
 // stores them at `d_args` (device) for the others; one graph replay
-// (captured once per length), or, with `ev`, plain launches with an event
-// before the first and after each.
-// Returns a cudaError_t.  Call with the library lock held.
-int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev = nullptr);
-// destroys the cached graphs (library shutdown)
-void fft_release_graphs();
+// (captured on `cap` once per length and argument buffer), or, with `ev`
+// (or without `cap`), plain launches with an event before the first and
+// after each.  Returns a cudaError_t.  The caller runs one product at a
+// time per argument buffer (its library lane's lock).
+int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* ev = nullptr,
+               cudaStream_t cap = nullptr);
+// destroys the cached graphs of one argument buffer (a lane's), or all
+void fft_release_graphs(const FftArgs* d_args = nullptr);
 
 }  // namespace precgpu

@@ -1,13 +1,17 @@
 // ntt_cols.cuh -- column passes of the four-step NTT (index i = i1*N2 + i2).
 //
 // k_fwd_cols: for C adjacent columns i2 of one operand and one prime, the
-//   limbs are read as 32-bit digits (set 2: whole 64-bit limbs) (the reference's ntt_digits and mont_in,
-//   src/mul_ntt.cpp:331-342, 357-360, fused into the load), reduced, run
-//   through a DIF transform over i1 (the first log2(N1) stages of
-//   ntt_forward, mul_ntt.cpp:193-255) and multiplied by the four-step
-//   twiddle w_N^(i2*k1).  Output row slot s holds frequency k1 = bitrev(s).
-// k_inv_cols: the DIT transform over the row slots (the last stages of
-//   ntt_inverse, mul_ntt.cpp:257-329) back to natural coefficient order.
+//   limbs are read as 32-bit digits (sets 2 and 3: whole 64-bit limbs) (the
+//   reference's ntt_digits and mont_in, src/mul_ntt.cpp:331-342, 357-360,
+//   fused into the load), reduced, run through a DIF transform over i1 (the
+//   first log2(N1) stages of ntt_forward, mul_ntt.cpp:193-255) and
+//   multiplied by the four-step twiddle w_N^(i2*k1).  Output row slot s
+//   holds frequency k1 = bitrev(s).
+// k_inv_cols: the inverse four-step twiddle w_N^-(i2*k1), then the DIT
+//   transform over the row slots (the last stages of ntt_inverse,
+//   mul_ntt.cpp:257-329) back to natural coefficient order.
+// Both generate their twiddles as running Montgomery powers over a thread's
+// 32 slots of one column (twiddle32).
 // Columns are interleaved in shared memory (element i of column c at
 // P(i)*C + c); a warp covers C columns x 32/C items, so every global access
 // moves whole 32-byte sectors.
@@ -121,14 +125,9 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs arg
             // slot 32u + q holds k1 = brev5(q) << (M-5) | brev(u): the twiddle
             // w^(i2*k1) is t * g^brev5(q) with t = w^(i2*brev(u)), g = w^(i2 << (M-5))
             const uint32_t i2 = c0 + col;
-            uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), args.k);
+            const uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), args.k);
             const uint32_t g = fourstep_twiddle<SET>(args.f, prime, i2 << (M - 5), args.k);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int q = brev5(j);
-                x[0][q] = Ar<SET>::mul(x[0][q], t, pc);
-                if (j < 31) t = Ar<SET>::mul(t, g, pc);
-            }
+            twiddle32<SET>(x[0], t, g, pc);
 #pragma unroll
             for (int q = 0; q < 32; ++q) dst[(uint64_t)(32 * u + q) * N2 + i2] = x[0][q];
         }
@@ -150,7 +149,31 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_inv_cols(ProdArgs arg
     // the column tile, staged by 16-byte asynchronous copies
     stage_cols<M, C>(sm, wk, N2, c0, ~0ull);
     __syncthreads();
-    col_passes<SET, M, NP - 1, 1, true, C, MR>(sm, tw, pc);
+    {   // bottom DIT pass (bits 0..4) after the inverse four-step twiddle
+        using G = Geom<M, NP - 1, MR>;
+        static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
+        const uint32_t nmask = (uint32_t)((1ull << args.k) - 1);
+        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+            const int col = w & (C - 1);
+            const uint32_t u = w / C;
+            uint32_t* s = sm + (33 * u) * C + col;
+            uint32_t x[1][32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
+            // slot 32u + q holds k1 = brev5(q) << (M-5) | brev(u): the twiddle
+            // w^-(i2*k1) is t * g^brev5(q), t = w^-(i2*brev(u)), g = w^-(i2 << (M-5));
+            // the row pass left every value in the forward range
+            const uint32_t i2 = c0 + col;
+            const uint32_t t = fourstep_twiddle<SET>(args.f, prime, (0u - i2 * brev_bits(u, M - 5)) & nmask, args.k);
+            const uint32_t g = fourstep_twiddle<SET>(args.f, prime, (0u - (i2 << (M - 5))) & nmask, args.k);
+            twiddle32<SET>(x[0], t, g, pc);
+            regs_pass<SET, M, NP - 1, true, 1, MR>(x, u, tw, pc);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) s[q * C] = x[0][q];
+        }
+        __syncthreads();
+    }
+    col_passes<SET, M, NP - 2, 1, true, C, MR>(sm, tw, pc);
     {   // top DIT pass: natural row order i1, straight to HBM
         using G = Geom<M, 0, MR>;
         for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {

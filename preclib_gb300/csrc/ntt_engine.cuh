@@ -257,17 +257,24 @@ __device__ __forceinline__ void stage_rows(uint32_t* sm, const uint32_t* __restr
 // rows i1 < 2^(M-1) of C columns; the low word of limb i1*ld + c0 + col
 // goes to row i1 and the high word to row i1 + 2^(M-1), the two elements
 // the top pass pairs anyway (limbs past `valid` read as zero).
+// Both words go by 4-byte asynchronous copies, all of a thread's copies in
+// flight at once (a load-then-store loop waited out the memory latency once
+// per limb: on GB300 that staging took 44% of the forward column pass).
 template <int M, int C>
 __device__ __forceinline__ void stage_limbs(uint32_t* sm, const uint64_t* __restrict__ g, uint64_t ld, uint64_t c0,
                                             uint64_t valid) {
     constexpr int H = 1 << (M - 1);
+    const uint32_t* __restrict__ g32 = reinterpret_cast<const uint32_t*>(g);
     for (int w = threadIdx.x; w < H * C; w += blockDim.x) {
         const int r = w / C, col = w % C;
         const uint64_t idx = (uint64_t)r * ld + c0 + col;
-        const uint64_t v = idx < valid ? __ldg(&g[idx]) : 0ull;
-        sm[padded(r) * C + col] = (uint32_t)v;
-        sm[padded(r + H) * C + col] = (uint32_t)(v >> 32);
+        const bool in = idx < valid;
+        const uint32_t* src = in ? g32 + 2 * idx : g32;  // 0 bytes read (zero fill) past the operand
+        cp_async4(sm + padded(r) * C + col, src, in ? 4 : 0);
+        cp_async4(sm + padded(r + H) * C + col, in ? src + 1 : g32, in ? 4 : 0);
     }
+    cp_async_commit();
+    cp_async_wait<0>();
 }
 
 template <int M, int C>
@@ -335,6 +342,20 @@ __device__ __forceinline__ uint32_t fourstep_twiddle(const FieldArgs& f, int pri
     const uint32_t hi = __ldg(&f.twhi[prime][E >> kTwLevelBits]);
     const uint32_t lo = __ldg(&f.twlo[prime][E & ((1u << kTwLevelBits) - 1)]);
     return Ar<SET>::mul(hi, lo, f.pc[prime]);
+}
+
+// x[brev5(j)] *= t * g^j for j = 0 .. 31 (t, g in Montgomery form; [0, 2p)
+// under set 0's arithmetic): the four-step twiddles of a thread's 32 slots
+// of one column as a running power.  (Four interleaved chains stepping by
+// g^4 measured no faster on GB300: the chain is not latency-bound.)
+template <int SET>
+__device__ __forceinline__ void twiddle32(uint32_t (&x)[32], uint32_t t, uint32_t g, const PrimeC& pc) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int q = brev5(j);
+        x[q] = Ar<SET>::mul(x[q], t, pc);
+        if (j < 31) t = Ar<SET>::mul(t, g, pc);
+    }
 }
 
 // ---------------------------------------------------------------------------

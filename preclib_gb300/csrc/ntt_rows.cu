@@ -1,12 +1,14 @@
 // ntt_rows.cu -- row pass of the four-step NTT.
 //
-// For `rows` row slots s of one prime: the remaining DIF stages of both
+// For `rows` row slots of one prime: the remaining DIF stages of both
 // operands' rows (the last log2(N2) stages of ntt_forward,
-// src/mul_ntt.cpp:193-255), the pointwise product (mul_ntt.cpp:364-373),
-// the first DIT stages of the product row (ntt_inverse, mul_ntt.cpp:257-311)
-// and the inverse four-step twiddle w_N^-(i2*k1), k1 = bitrev(s).  The
-// bottom five stages of both directions and the product run in registers
-// without a shared-memory round trip in between.
+// src/mul_ntt.cpp:193-255), the pointwise product (mul_ntt.cpp:364-373)
+// and the first DIT stages of the product row (ntt_inverse,
+// mul_ntt.cpp:257-311).  The bottom five stages of both directions and the
+// product run in registers without a shared-memory round trip in between.
+// The four-step twiddles are the column passes' (the inverse one measured
+// 1-2% faster at 2^21 points in the inverse column pass, where it shares the
+// loop over a thread's 32 slots with the forward one's pattern).
 // pass radix cap of the row transforms (radix-8/16 passes: two operands'
 // radix-64 items would not fit the register budget)
 #ifndef PREC_ROWS_MAXRB
@@ -23,13 +25,8 @@
 #ifndef PREC_ROWS_THREADS
 #define PREC_ROWS_THREADS 64
 #endif
-#ifndef PREC_ROWS_TOP_UNROLL
-#define PREC_ROWS_TOP_UNROLL 1
-#endif
 
 namespace precgpu {
-
-constexpr int kRowsTopUnroll = PREC_ROWS_TOP_UNROLL;  // items of the top pass in flight per thread
 
 // MR: pass radix cap.  With MR = 6 a 2^11-point row runs as a radix-64 and
 // a radix-32 pass (no middle pass); the radix-64 top pass then takes the two
@@ -51,12 +48,14 @@ __global__ void __launch_bounds__(256, MR == 6 ? 2 : PREC_ROWS_MINB) k_rows(Prod
     const uint32_t row0 = blockIdx.x * rows;
     constexpr int NA = SQ ? 1 : 2;  // a square transforms its one operand only
 
-    {   // top DIF pass of A (and B) straight from HBM (shared twiddles)
+    {   // top DIF pass of A (and B) straight from HBM (shared twiddles).
+        // (Staging the rows into shared memory first by 4-byte asynchronous
+        // copies -- the padding leaves no 16-byte alignment -- measured slower
+        // on GB300: 78 against 70 us at 2^21 points.)
         using G = Geom<M, 0, MR>;
         constexpr bool SEQ = !SQ && G::R > 32;  // operands one after the other
         constexpr int NT = SEQ ? 1 : NA;        // operands per item
         constexpr int items = 1 << G::LGI;
-#pragma unroll kRowsTopUnroll
         for (int w = threadIdx.x; w < (rows * items) * (SEQ ? 2 : 1); w += blockDim.x) {
             const int op = SEQ ? w / (rows * items) : 0;
             const int wi = SEQ ? w - op * (rows * items) : w;
@@ -106,9 +105,8 @@ __global__ void __launch_bounds__(256, MR == 6 ? 2 : PREC_ROWS_MINB) k_rows(Prod
         __syncthreads();
     }
     row_passes<SET, M, NP - 2, 1, true, 1, MR>(sm, 2 * AS, rows, twi, pc);
-    {   // top DIT pass with the inverse four-step twiddle, straight to HBM
+    {   // top DIT pass, straight to HBM
         using G = Geom<M, 0, MR>;
-        const uint32_t nmask = (uint32_t)((1ull << args.k) - 1);
         for (int w = threadIdx.x; w < (rows << G::LGI); w += blockDim.x) {
             const int r = w >> G::LGI;
             const uint32_t u = w & ((1u << G::LGI) - 1);
@@ -117,18 +115,11 @@ __global__ void __launch_bounds__(256, MR == 6 ? 2 : PREC_ROWS_MINB) k_rows(Prod
 #pragma unroll
             for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS];
             regs_pass<SET, M, 0, true, 1, MR>(x, u, twi, pc);
-            // element q is i2 = base + (q << LO); twiddle w^-(i2*k1) = t * g^q
-            const uint32_t srow = row0 + r;
-            const uint32_t k1v = brev_bits(srow, args.k1);
-            const uint32_t base = G::base(u);
-            uint32_t t = fourstep_twiddle<SET>(args.f, prime, (0u - base * k1v) & nmask, args.k);
-            const uint32_t g = fourstep_twiddle<SET>(args.f, prime, (0u - (k1v << G::LO)) & nmask, args.k);
-            uint32_t* __restrict__ dst = A + ((uint64_t)srow << M) + base;
+            // in the forward range: the inverse column pass multiplies by the
+            // inverse four-step twiddle first
+            uint32_t* __restrict__ dst = A + ((uint64_t)(row0 + r) << M) + G::base(u);
 #pragma unroll
-            for (int q = 0; q < G::R; ++q) {
-                dst[(uint32_t)q << G::LO] = Ar<SET>::mul(Ar<SET>::half(x[0][q], pc), t, pc);
-                if (q < G::R - 1) t = Ar<SET>::mul(t, g, pc);
-            }
+            for (int q = 0; q < G::R; ++q) dst[(uint32_t)q << G::LO] = Ar<SET>::half(x[0][q], pc);
         }
     }
 }

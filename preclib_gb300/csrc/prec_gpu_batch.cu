@@ -299,6 +299,7 @@ int prec_gpu_batch_create(const prec_gpu_product_t* items, size_t count, prec_gp
 
 int prec_gpu_batch_run(prec_gpu_batch_t* b, void* stream) {
     if (!b) return PREC_GPU_E_ARG;
+    NvtxRange range("prec_gpu_batch_run %zu products, %zu classes", b->items.size(), b->classes.size());
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (!b->exec) {
         cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);

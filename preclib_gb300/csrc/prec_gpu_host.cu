@@ -6,8 +6,10 @@
 //     src/mul_ntt.cpp:37-41 and rebuilds root tables per size in
 //     ntt_build_roots, mul_ntt.cpp:150-191; here one 2^13-entry table per
 //     prime and direction serves every transform length);
-//   * a workspace that grows to the largest product seen;
-//   * one stream for the host-pointer entry points.
+//   * per calling thread, a lane (Lane): a stream for the host-pointer
+//     entry points, a workspace and staging buffers that grow to the
+//     largest product the thread has made, and its captured graphs, so
+//     products from different threads overlap on the device.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -264,39 +267,58 @@ struct GraphEntry {
     cudaGraph_t graph = nullptr;  // kept: a node's parameters are set through its graph's node handle
 };
 
-struct Ctx {
+// One calling thread's resources (a "lane"): its streams, the per-product
+// workspace and staging buffers, the status block a host product reads
+// back, events, per-prime streams and captured single-product graphs.
+// Products on different lanes run concurrently on the GPU; a lane runs one
+// product at a time (mu).  A thread takes a lane on its first call and
+// keeps it; past kMaxLanes threads, threads share lanes round-robin.  (The
+// reference's multiply is per thread the same way: its NTT plans are
+// thread_local, src/mul_ntt.cpp:182-191.)
+constexpr int kMaxLanes = 16;
+struct Lane {
     std::mutex mu;
-    bool ready = false;
-    int device = -1;
-    cudaStream_t stream = nullptr;
-    void* tables = nullptr;
+    cudaStream_t stream = nullptr;  // host-pointer products
+    cudaStream_t cap = nullptr;     // capture stream of this lane's graphs
+    // host products with a chunked CRT: each chunk's limbs copy out on
+    // `copy` while the next chunks run
+    cudaStream_t copy = nullptr;
     uint8_t* ws = nullptr;
     size_t ws_cap = 0;
     uint64_t* io = nullptr;
-    size_t io_cap = 0;  // limbs
+    size_t io_cap = 0;        // limbs
     uint64_t* blk = nullptr;  // blocked products: a block pair's product, then the add kernel's scratch
     size_t blk_cap = 0;       // limbs
-    int* d_err = nullptr;      // device status: error bits at +0, FFT max distance at +8
-    int* h_err = nullptr;      // pinned copy of the status
+    int* d_err = nullptr;     // host products' device status: error bits at +0, FFT max distance at +8
+    int* h_err = nullptr;     // pinned copy of the status
     double* d_maxdist = nullptr;
     double* h_maxdist = nullptr;
-    double2* fft_tw = nullptr;  // FP64 band twiddles
     FftArgs* fft_args = nullptr;  // the FP64 band product's arguments, read by its kernels
     cudaEvent_t last_done = nullptr, ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // each operand on the device
     cudaEvent_t stage_ev[kMaxStages + 1] = {};
-    FieldArgs field[kSets] = {};
-    PrimeStreams prime_streams = {};
-    cudaMemPool_t pool = nullptr;
-    bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
-    std::map<GraphKey, GraphEntry> graphs;  // single-product graphs by plan shape
-    cudaStream_t cap = nullptr;             // their capture stream
-    // host products with a chunked CRT: each chunk's limbs copy out on
-    // `copy` while the next chunks run
-    cudaStream_t copy = nullptr;
     cudaEvent_t chunk_done[kCrtMaxChunks] = {};
     cudaEvent_t copy_done = nullptr;
     uint32_t* chunk_words = nullptr;  // 2 * kCrtMaxChunks words
+    PrimeStreams prime_streams = {};
+    std::map<GraphKey, GraphEntry> graphs;  // single-product graphs by plan shape
+};
+
+struct Ctx {
+    std::mutex mu;  // initialisation, the lane list, the shared error word
+    std::atomic<bool> ready{false};
+    int device = -1;
+    void* tables = nullptr;
+    // library-wide device error word (device-pointer products, batches, the
+    // tuner; read by prec_gpu_stream_check) and its pinned copy
+    int* d_err = nullptr;
+    int* h_err = nullptr;
+    double2* fft_tw = nullptr;  // FP64 band twiddles
+    FieldArgs field[kSets] = {};
+    cudaMemPool_t pool = nullptr;
+    bool split_primes = true;  // PREC_GPU_PRIME_STREAMS=0 runs the primes in one launch per kernel
+    std::vector<std::unique_ptr<Lane>> lanes;
+    std::atomic<uint64_t> gen{0};  // bumped by shutdown: threads then take new lanes
 };
 
 // 64-bit digits (set 2) for single products: on unless PREC_GPU_WIDE_DIGITS=0;
@@ -412,23 +434,6 @@ static int init_locked(Ctx& c, int device) {
     if (device >= n) return PREC_GPU_E_ARG;
     CK(cudaSetDevice(device));
     c.device = device;
-    CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
-    for (int i = 0; i < kCrtMaxChunks; ++i) CK(cudaEventCreateWithFlags(&c.chunk_done[i], cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&c.copy_done, cudaEventDisableTiming));
-    CK(cudaMalloc(&c.chunk_words, 2 * kCrtMaxChunks * sizeof(uint32_t)));
-    CK(cudaEventCreateWithFlags(&c.last_done, cudaEventDisableTiming));
-    CK(cudaEventCreate(&c.ev0));
-    CK(cudaEventCreate(&c.ev1));
-    CK(cudaEventCreateWithFlags(&c.ev_a, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&c.ev_b, cudaEventDisableTiming));
-    for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&c.stage_ev[i]));
-    for (int p = 0; p < kMaxPrimes; ++p) {
-        CK(cudaStreamCreateWithFlags(&c.prime_streams.s[p], cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&c.prime_streams.join[p], cudaEventDisableTiming));
-    }
-    CK(cudaEventCreateWithFlags(&c.prime_streams.fork, cudaEventDisableTiming));
     {
         cudaMemPoolProps props{};
         props.allocType = cudaMemAllocationTypePinned;
@@ -445,23 +450,119 @@ static int init_locked(Ctx& c, int device) {
     CK(cudaMalloc(&c.d_err, kStatBytes));
     CK(cudaMemset(c.d_err, 0, kStatBytes));
     CK(cudaMallocHost(&c.h_err, kStatBytes));
-    c.d_maxdist = reinterpret_cast<double*>(reinterpret_cast<char*>(c.d_err) + 8);
-    c.h_maxdist = reinterpret_cast<double*>(reinterpret_cast<char*>(c.h_err) + 8);
     CK((cudaError_t)ntt_configure_kernels());
     CK((cudaError_t)fft_configure_kernels());
     CK(cudaMalloc(&c.fft_tw, fft_table_bytes()));
-    CK(cudaMalloc(&c.fft_args, sizeof(FftArgs)));
-    fft_build_table(c.fft_tw, c.stream);
+    fft_build_table(c.fft_tw, nullptr);
     CK(cudaGetLastError());
     int r = build_tables(c);
     if (r) return r;
     CK(cudaDeviceSynchronize());
-    c.ready = true;
+    c.ready.store(true, std::memory_order_release);
     // a saved tuning table (an invalid file leaves the defaults in place)
     if (const char* tf = std::getenv("PREC_GPU_TUNE_FILE")) {
         if (prec_gpu_tune_load(tf) != PREC_GPU_OK) std::fprintf(stderr, "prec_gpu: ignoring tuning table %s\n", tf);
     }
     return 0;
+}
+
+static void lane_destroy(Lane& L) {
+    if (L.stream) cudaStreamSynchronize(L.stream);
+    for (auto& kv : L.graphs) {
+        cudaGraphExecDestroy(kv.second.exec);
+        cudaGraphDestroy(kv.second.graph);
+        cudaFree(kv.second.d_desc);
+    }
+    L.graphs.clear();
+    cudaFree(L.ws);
+    cudaFree(L.io);
+    cudaFree(L.blk);
+    cudaFree(L.d_err);
+    cudaFreeHost(L.h_err);
+    cudaFree(L.fft_args);
+    cudaFree(L.chunk_words);
+    for (cudaEvent_t e : {L.last_done, L.ev0, L.ev1, L.ev_a, L.ev_b, L.copy_done})
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : L.stage_ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : L.chunk_done)
+        if (e) cudaEventDestroy(e);
+    for (int p = 0; p < kMaxPrimes; ++p) {
+        if (L.prime_streams.s[p]) cudaStreamDestroy(L.prime_streams.s[p]);
+        if (L.prime_streams.join[p]) cudaEventDestroy(L.prime_streams.join[p]);
+    }
+    if (L.prime_streams.fork) cudaEventDestroy(L.prime_streams.fork);
+    for (cudaStream_t s : {L.stream, L.cap, L.copy})
+        if (s) cudaStreamDestroy(s);
+    fft_release_graphs(L.fft_args);
+}
+
+static int lane_create(Lane& L) {
+    CK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&L.cap, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&L.copy, cudaStreamNonBlocking));
+    for (int i = 0; i < kCrtMaxChunks; ++i) CK(cudaEventCreateWithFlags(&L.chunk_done[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&L.copy_done, cudaEventDisableTiming));
+    CK(cudaMalloc(&L.chunk_words, 2 * kCrtMaxChunks * sizeof(uint32_t)));
+    CK(cudaEventCreateWithFlags(&L.last_done, cudaEventDisableTiming));
+    CK(cudaEventCreate(&L.ev0));
+    CK(cudaEventCreate(&L.ev1));
+    CK(cudaEventCreateWithFlags(&L.ev_a, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&L.ev_b, cudaEventDisableTiming));
+    for (int i = 0; i <= kMaxStages; ++i) CK(cudaEventCreate(&L.stage_ev[i]));
+    for (int p = 0; p < kMaxPrimes; ++p) {
+        CK(cudaStreamCreateWithFlags(&L.prime_streams.s[p], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&L.prime_streams.join[p], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&L.prime_streams.fork, cudaEventDisableTiming));
+    CK(cudaMalloc(&L.d_err, kStatBytes));
+    CK(cudaMemset(L.d_err, 0, kStatBytes));
+    CK(cudaMallocHost(&L.h_err, kStatBytes));
+    L.d_maxdist = reinterpret_cast<double*>(reinterpret_cast<char*>(L.d_err) + 8);
+    L.h_maxdist = reinterpret_cast<double*>(reinterpret_cast<char*>(L.h_err) + 8);
+    CK(cudaMalloc(&L.fft_args, sizeof(FftArgs)));
+    return 0;
+}
+
+static thread_local Lane* t_lane = nullptr;
+static thread_local uint64_t t_lane_gen = ~0ull;
+static std::atomic<uint64_t> g_lane_rr{0};
+
+// The calling thread's lane, the context initialised first (context lock
+// held by the caller).
+static int thread_lane_locked(Ctx& c, int device, Lane*& out) {
+    int r = init_locked(c, device);
+    if (r) return r;
+    const uint64_t gen = c.gen.load(std::memory_order_relaxed);
+    if (!t_lane || t_lane_gen != gen) {
+        Lane* L = nullptr;
+        if ((int)c.lanes.size() < kMaxLanes) {
+            std::unique_ptr<Lane> p(new Lane());
+            if ((r = lane_create(*p))) {
+                lane_destroy(*p);
+                return r;
+            }
+            L = p.get();
+            c.lanes.push_back(std::move(p));
+        } else {
+            L = c.lanes[g_lane_rr.fetch_add(1, std::memory_order_relaxed) % kMaxLanes].get();
+        }
+        t_lane = L;
+        t_lane_gen = gen;
+    }
+    out = t_lane;
+    return 0;
+}
+
+// The calling thread's lane (takes the context lock only on the thread's
+// first call and after a shutdown).
+static int thread_lane(Ctx& c, Lane*& out) {
+    if (t_lane && c.ready.load(std::memory_order_acquire) && t_lane_gen == c.gen.load(std::memory_order_relaxed)) {
+        out = t_lane;
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(c.mu);
+    return thread_lane_locked(c, -1, out);
 }
 
 std::mutex& ctx_mutex() { return g_ctx.mu; }
@@ -487,57 +588,44 @@ int ctx_take_device_err() {
 int* ctx_device_err() { return g_ctx.d_err; }
 cudaMemPool_t ctx_pool() { return g_ctx.pool; }
 
-static int ensure_ws(Ctx& c, size_t bytes) {
-    if (bytes <= c.ws_cap) return 0;
-    if (c.ws) {
+// The lane's buffers grow to the largest product it has seen.  (A grown
+// buffer is freed after the device is idle: earlier products of this lane
+// may have been enqueued on callers' streams.)
+static int grow(void** buf, size_t* cap, size_t bytes, bool slack) {
+    if (bytes <= *cap) return 0;
+    if (*buf) {
         CK(cudaDeviceSynchronize());
-        cudaFree(c.ws);
-        c.ws = nullptr;
-        c.ws_cap = 0;
+        cudaFree(*buf);
+        *buf = nullptr;
+        *cap = 0;
     }
-    size_t cap = std::max(bytes, c.ws_cap * 3 / 2);
-    if (cudaMalloc(&c.ws, cap) != cudaSuccess) {
+    size_t want = slack ? std::max(bytes, bytes + bytes / 2) : bytes;
+    if (cudaMalloc(buf, want) != cudaSuccess) {
         cudaGetLastError();
-        if (cudaMalloc(&c.ws, bytes) != cudaSuccess) {
+        if (want == bytes || cudaMalloc(buf, bytes) != cudaSuccess) {
             cudaGetLastError();
             return PREC_GPU_E_NOMEM;
         }
-        cap = bytes;
+        want = bytes;
     }
-    c.ws_cap = cap;
+    *cap = want;
     return 0;
 }
 
-static int ensure_blk(Ctx& c, size_t limbs) {
-    if (limbs <= c.blk_cap) return 0;
-    if (c.blk) {
-        CK(cudaDeviceSynchronize());
-        cudaFree(c.blk);
-        c.blk = nullptr;
-        c.blk_cap = 0;
-    }
-    if (cudaMalloc(&c.blk, limbs * sizeof(uint64_t)) != cudaSuccess) {
-        cudaGetLastError();
-        return PREC_GPU_E_NOMEM;
-    }
-    c.blk_cap = limbs;
-    return 0;
+static int ensure_ws(Lane& L, size_t bytes) { return grow(reinterpret_cast<void**>(&L.ws), &L.ws_cap, bytes, true); }
+
+static int ensure_blk(Lane& L, size_t limbs) {
+    size_t cap = L.blk_cap * sizeof(uint64_t);
+    const int r = grow(reinterpret_cast<void**>(&L.blk), &cap, limbs * sizeof(uint64_t), false);
+    L.blk_cap = cap / sizeof(uint64_t);
+    return r;
 }
 
-static int ensure_io(Ctx& c, size_t limbs) {
-    if (limbs <= c.io_cap) return 0;
-    if (c.io) {
-        CK(cudaDeviceSynchronize());
-        cudaFree(c.io);
-        c.io = nullptr;
-        c.io_cap = 0;
-    }
-    if (cudaMalloc(&c.io, limbs * sizeof(uint64_t)) != cudaSuccess) {
-        cudaGetLastError();
-        return PREC_GPU_E_NOMEM;
-    }
-    c.io_cap = limbs;
-    return 0;
+static int ensure_io(Lane& L, size_t limbs) {
+    size_t cap = L.io_cap * sizeof(uint64_t);
+    const int r = grow(reinterpret_cast<void**>(&L.io), &cap, limbs * sizeof(uint64_t), false);
+    L.io_cap = cap / sizeof(uint64_t);
+    return r;
 }
 
 // Enqueues one NTT-band product on device pointers.
@@ -549,10 +637,10 @@ static int ensure_io(Ctx& c, size_t limbs) {
 // inverse column and carry kernels, which run in batch form on it.  (An
 // upload of the descriptor by a copy in the stream measured 8-10 us slower
 // per product when the caller's operands were page-locked.)
-static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStream_t st) {
+static int enqueue_graph(Lane& L, const ProdArgs& args, const Plan& pl, cudaStream_t st) {
     const GraphKey key{pl.set, pl.k, pl.k1, pl.cg, pl.cmr, pl.rmr, pl.rows, args.square};
-    auto it = c.graphs.find(key);
-    if (it == c.graphs.end()) {
+    auto it = L.graphs.find(key);
+    if (it == L.graphs.end()) {
         GraphEntry e;
         CK(cudaMalloc(&e.d_desc, sizeof(ProdPtrs)));
         ProdArgs first = args;
@@ -564,20 +652,20 @@ static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStrea
         const uint64_t lout_max = set_wide(pl.set) ? (1ull << pl.k) + 1 : (1ull << pl.k) / 2 + 1;
         const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
         const int max_nblk = (int)((lout_max + bl - 1) / bl);
-        cudaError_t err = cudaStreamBeginCapture(c.cap, cudaStreamCaptureModeThreadLocal);
+        cudaError_t err = cudaStreamBeginCapture(L.cap, cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) {
             cudaFree(e.d_desc);
             return cuda_code(err);
         }
         const uint64_t before = launches_this_thread();
-        launch_fwd_cols(pl.set, first, c.cap);
-        launch_rows(pl.set, cls, c.cap, e.d_desc, 1);
-        launch_inv_cols(pl.set, cls, c.cap, e.d_desc, 1);
-        launch_crt_carry(pl.set, cls, c.cap, e.d_desc, 1, max_nblk);
+        launch_fwd_cols(pl.set, first, L.cap);
+        launch_rows(pl.set, cls, L.cap, e.d_desc, 1);
+        launch_inv_cols(pl.set, cls, L.cap, e.d_desc, 1);
+        launch_crt_carry(pl.set, cls, L.cap, e.d_desc, 1, max_nblk);
         e.launches = launches_this_thread() - before;  // captured, counted at every replay
         uncount_launches(e.launches);
         cudaGraph_t g = nullptr;
-        err = cudaStreamEndCapture(c.cap, &g);
+        err = cudaStreamEndCapture(L.cap, &g);
         // the forward column node: the graph's only node without a dependency
         size_t n = 0;
         if (err == cudaSuccess) err = cudaGraphGetRootNodes(g, nullptr, &n);
@@ -593,7 +681,7 @@ static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStrea
             return cuda_code(err);
         }
         e.graph = g;
-        it = c.graphs.emplace(key, e).first;
+        it = L.graphs.emplace(key, e).first;
     }
     GraphEntry& e = it->second;
     ProdArgs first = args;
@@ -609,8 +697,10 @@ static int enqueue_graph(Ctx& c, const ProdArgs& args, const Plan& pl, cudaStrea
     return 0;
 }
 
-static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
-                       uint64_t* d_out, const Plan& pl, cudaStream_t st, cudaEvent_t* ev = nullptr,
+// Device error bits go to `err` (the lane's status block for host
+// products, the library-wide word otherwise).
+static int enqueue_ntt(Ctx& c, Lane& L, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
+                       uint64_t* d_out, const Plan& pl, cudaStream_t st, int* err, cudaEvent_t* ev = nullptr,
                        cudaEvent_t a_ready = nullptr, cudaEvent_t b_ready = nullptr,
                        const CrtChunks* chunks = nullptr) {
     const int square = (d_a == d_b && la == lb) ? 1 : 0;
@@ -632,9 +722,9 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         args.a = d_a;
         args.b = d_b;
         args.out = d_out;
-        args.work = reinterpret_cast<uint32_t*>(c.ws);
+        args.work = reinterpret_cast<uint32_t*>(L.ws);
         args.scratch = args.work + ((size_t)2 * pl.nprimes << pl.k);
-        args.err = c.d_err;
+        args.err = err;
         args.la = la;
         args.lb = lb;
         args.lout = lout;
@@ -656,8 +746,8 @@ static int enqueue_ntt(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t*
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         if (!split && !ev && pl.k <= kGraphMaxLog2 && cudaStreamIsCapturing(st, &cap) == cudaSuccess &&
             cap == cudaStreamCaptureStatusNone)
-            return enqueue_graph(c, args, pl, st);
-        ntt_launch_4step(pl.set, args, st, ev, split ? &c.prime_streams : nullptr, a_ready, b_ready,
+            return enqueue_graph(L, args, pl, st);
+        ntt_launch_4step(pl.set, args, st, ev, split ? &L.prime_streams : nullptr, a_ready, b_ready,
                          split ? chunks : nullptr);
     }
     CK(cudaGetLastError());
@@ -681,7 +771,7 @@ static uint64_t block_limbs() { return g_block_limbs.load(std::memory_order_rela
 // Device memory of a blocked product (the workspace of every block shape --
 // whole blocks and the remainders -- and the temporary); `top` gets the
 // plan of a whole block pair.
-static int prepare_blocked(Ctx& c, uint64_t la, uint64_t lb, uint64_t B, Plan& top) {
+static int prepare_blocked(Lane& L, uint64_t la, uint64_t lb, uint64_t B, Plan& top) {
     const uint64_t sa[2] = {std::min(B, la), la % B}, sb[2] = {std::min(B, lb), lb % B};
     size_t ws = 0;
     for (int x = 0; x < 2; ++x)
@@ -694,18 +784,18 @@ static int prepare_blocked(Ctx& c, uint64_t la, uint64_t lb, uint64_t B, Plan& t
             if (x == 0 && y == 0) top = pl;
         }
     const uint64_t tl = sa[0] + sb[0];
-    int r = ensure_ws(c, ws);
-    if (!r) r = ensure_blk(c, tl + (add_into_scratch_words(tl) + 1) / 2);
+    int r = ensure_ws(L, ws);
+    if (!r) r = ensure_blk(L, tl + (add_into_scratch_words(tl) + 1) / 2);
     return r;
 }
 
 // Enqueues a blocked product (after prepare_blocked for the same sizes).
-static int enqueue_blocked(Ctx& c, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
-                           uint64_t* d_out, cudaStream_t st, uint64_t B) {
+static int enqueue_blocked(Ctx& c, Lane& L, const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb,
+                           uint64_t* d_out, cudaStream_t st, uint64_t B, int* err) {
     const uint64_t lout = la + lb;
     const uint64_t tl = std::min(B, la) + std::min(B, lb);
-    uint64_t* tmp = c.blk;
-    uint32_t* scratch = reinterpret_cast<uint32_t*>(c.blk + tl);
+    uint64_t* tmp = L.blk;
+    uint32_t* scratch = reinterpret_cast<uint32_t*>(L.blk + tl);
     int r = 0;
     CK(cudaMemsetAsync(d_out, 0, lout * sizeof(uint64_t), st));
     for (uint64_t i = 0; i < la; i += B)
@@ -713,8 +803,8 @@ static int enqueue_blocked(Ctx& c, const uint64_t* d_a, uint64_t la, const uint6
             const uint64_t na = std::min(B, la - i), nb = std::min(B, lb - j);
             Plan pl;
             if ((r = plan_for(2 * na, 2 * nb, na + nb, pl, wide_digits()))) return r;
-            if ((r = enqueue_ntt(c, d_a + i, na, d_b + j, nb, tmp, pl, st))) return r;
-            launch_add_into(d_out + i + j, lout - i - j, tmp, na + nb, scratch, c.d_err, st);
+            if ((r = enqueue_ntt(c, L, d_a + i, na, d_b + j, nb, tmp, pl, st, err))) return r;
+            launch_add_into(d_out + i + j, lout - i - j, tmp, na + nb, scratch, err, st);
         }
     CK(cudaGetLastError());
     return 0;
@@ -722,10 +812,20 @@ static int enqueue_blocked(Ctx& c, const uint64_t* d_a, uint64_t la, const uint6
 
 int ctx_enqueue_ntt_locked(const uint64_t* d_a, uint64_t la, const uint64_t* d_b, uint64_t lb, uint64_t* d_out,
                            const Plan& pl, cudaStream_t st) {
-    return enqueue_ntt(g_ctx, d_a, la, d_b, lb, d_out, pl, st);
+    Lane* L = nullptr;
+    int r = thread_lane_locked(g_ctx, -1, L);
+    if (r) return r;
+    std::lock_guard<std::mutex> lk(L->mu);
+    return enqueue_ntt(g_ctx, *L, d_a, la, d_b, lb, d_out, pl, st, g_ctx.d_err);
 }
 
-int ctx_ensure_ws_locked(size_t bytes) { return ensure_ws(g_ctx, bytes); }
+int ctx_ensure_ws_locked(size_t bytes) {
+    Lane* L = nullptr;
+    int r = thread_lane_locked(g_ctx, -1, L);
+    if (r) return r;
+    std::lock_guard<std::mutex> lk(L->mu);
+    return ensure_ws(*L, bytes);
+}
 
 static size_t trim(const uint64_t* a, size_t n) {
     while (n > 0 && a[n - 1] == 0) --n;
@@ -800,9 +900,11 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     if ((!a && an) || (!b && bn) || (!out && an + bn)) return PREC_GPU_E_ARG;
     const bool square = a == b && an == bn;
     Ctx& c = g_ctx;
-    std::lock_guard<std::mutex> lk(c.mu);
-    int r = init_locked(c, -1);
+    Lane* lp = nullptr;
+    int r = thread_lane(c, lp);
     if (r) return r;
+    Lane& L = *lp;
+    std::lock_guard<std::mutex> lk(L.mu);
     const size_t total = an + bn;
     const size_t la = a ? trim(a, an) : 0, lb = b ? trim(b, bn) : 0;
     memset(&t_stats, 0, sizeof(t_stats));
@@ -826,35 +928,37 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
     const bool blocked = !use_fft && hi > B;
     Plan pl;
     if (blocked) {
-        if ((r = prepare_blocked(c, la, lb, B, pl))) return r;
+        if ((r = prepare_blocked(L, la, lb, B, pl))) return r;
     } else {
         if (!use_fft && (r = plan_for(digits32(a, la), digits32(b, lb), lout, pl, wide_digits()))) return r;
-        if ((r = ensure_ws(c, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
+        if ((r = ensure_ws(L, use_fft ? fp.work_bytes : pl.work_bytes))) return r;
     }
     // operands and result each start on a 256-byte boundary (32 limbs)
     const size_t la_pad = (la + 31) & ~(size_t)31, lb_pad = square ? 0 : (lb + 31) & ~(size_t)31;
-    if ((r = ensure_io(c, la_pad + lb_pad + lout))) return r;
-    uint64_t* d_a = c.io;
-    uint64_t* d_b = square ? d_a : c.io + la_pad;
-    uint64_t* d_out = c.io + la_pad + lb_pad;
-    cudaStream_t st = c.stream;
-    CK(cudaStreamWaitEvent(st, c.last_done, 0));
+    if ((r = ensure_io(L, la_pad + lb_pad + lout))) return r;
+    uint64_t* d_a = L.io;
+    uint64_t* d_b = square ? d_a : L.io + la_pad;
+    uint64_t* d_out = L.io + la_pad + lb_pad;
+    cudaStream_t st = L.stream;
+    NvtxRange range("prec_gpu_mul %zux%zu %s", la, lb, use_fft ? "fft" : (blocked ? "blocked" : "ntt"));
+    CK(cudaStreamWaitEvent(st, L.last_done, 0));
     // the per-prime chains start on a's forward columns while b is copied
     CK(cudaMemcpyAsync(d_a, a, la * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    CK(cudaEventRecord(c.ev_a, st));
+    CK(cudaEventRecord(L.ev_a, st));
     if (!square) CK(cudaMemcpyAsync(d_b, b, lb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    CK(cudaEventRecord(c.ev_b, st));
-    CK(cudaEventRecord(c.ev0, st));
+    CK(cudaEventRecord(L.ev_b, st));
+    CK(cudaEventRecord(L.ev0, st));
     bool copied = false;  // the result went out chunk by chunk
+    nvtxRangePushA("enqueue product");
     if (use_fft) {
         FftArgs f{};  // pageable: the small upload travels in the command stream
         f.a = d_a;
         f.bp = d_b;
         f.out = d_out;
-        f.work = reinterpret_cast<double2*>(c.ws);
-        f.coef = reinterpret_cast<long long*>(c.ws + (sizeof(double2) << fp.k));
-        f.maxdist = c.d_maxdist;
-        f.err = c.d_err;
+        f.work = reinterpret_cast<double2*>(L.ws);
+        f.coef = reinterpret_cast<long long*>(L.ws + (sizeof(double2) << fp.k));
+        f.maxdist = L.d_maxdist;
+        f.err = L.d_err;
         f.tw = c.fft_tw;
         f.la = la;
         f.lb = lb;
@@ -866,9 +970,9 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         f.k = fp.k;
         f.k1 = fp.k1;
         f.k2 = fp.k2;
-        CK((cudaError_t)fft_launch(f, c.fft_args, st));
+        CK((cudaError_t)fft_launch(f, L.fft_args, st, nullptr, L.cap));
     } else if (blocked) {
-        if ((r = enqueue_blocked(c, d_a, la, d_b, lb, d_out, st, B))) return r;
+        if ((r = enqueue_blocked(c, L, d_a, la, d_b, lb, d_out, st, B, L.d_err))) return r;
     } else {
         // a large product's CRT runs in limb chunks; each chunk's limbs copy
         // out on the copy stream while the next chunks run
@@ -877,49 +981,53 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         if (chunked) {
             const int per = (pl.nblk + kCrtMaxChunks - 1) / kCrtMaxChunks;
             ch.count = (pl.nblk + per - 1) / per;  // every chunk nonempty
-            ch.words = c.chunk_words;
+            ch.words = L.chunk_words;
             for (int i = 0; i <= ch.count; ++i) ch.blk0[i] = std::min(i * per, pl.nblk);
-            for (int i = 0; i < ch.count; ++i) ch.done[i] = c.chunk_done[i];
-            CK(cudaMemsetAsync(c.chunk_words, 0, 2 * kCrtMaxChunks * sizeof(uint32_t), st));
+            for (int i = 0; i < ch.count; ++i) ch.done[i] = L.chunk_done[i];
+            CK(cudaMemsetAsync(L.chunk_words, 0, 2 * kCrtMaxChunks * sizeof(uint32_t), st));
         }
-        if ((r = enqueue_ntt(c, d_a, la, d_b, lb, d_out, pl, st, nullptr, c.ev_a, c.ev_b, chunked ? &ch : nullptr)))
+        if ((r = enqueue_ntt(c, L, d_a, la, d_b, lb, d_out, pl, st, L.d_err, nullptr, L.ev_a, L.ev_b, chunked ? &ch : nullptr)))
             return r;
         if (chunked) {
             const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
             for (int i = 0; i < ch.count; ++i) {
                 const uint64_t lo = std::min((uint64_t)ch.blk0[i] * bl, lout);
                 const uint64_t hi = std::min((uint64_t)ch.blk0[i + 1] * bl, lout);
-                CK(cudaStreamWaitEvent(c.copy, ch.done[i], 0));
+                CK(cudaStreamWaitEvent(L.copy, ch.done[i], 0));
                 if (hi > lo)
                     CK(cudaMemcpyAsync(out + lo, d_out + lo, (hi - lo) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
-                                       c.copy));
+                                       L.copy));
             }
-            CK(cudaEventRecord(c.copy_done, c.copy));
+            CK(cudaEventRecord(L.copy_done, L.copy));
             copied = true;
         }
     }
-    CK(cudaEventRecord(c.ev1, st));
+    nvtxRangePop();
+    CK(cudaEventRecord(L.ev1, st));
     // error word and the FFT distance first: a failed product leaves `out` untouched
-    CK(cudaMemcpyAsync(c.h_err, c.d_err, kStatBytes, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemsetAsync(c.d_err, 0, sizeof(int), st));
+    CK(cudaMemcpyAsync(L.h_err, L.d_err, kStatBytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemsetAsync(L.d_err, 0, sizeof(int), st));
     if (use_fft) CK(cudaStreamSynchronize(st));
-    const bool fft_failed = use_fft && (*c.h_err & kDevErrFftRound);
-    if (copied) CK(cudaStreamWaitEvent(st, c.copy_done, 0));
+    const bool fft_failed = use_fft && (*L.h_err & kDevErrFftRound);
+    if (copied) CK(cudaStreamWaitEvent(st, L.copy_done, 0));
     else if (!fft_failed) CK(cudaMemcpyAsync(out, d_out, lout * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaEventRecord(c.last_done, st));
-    CK(cudaStreamSynchronize(st));
+    CK(cudaEventRecord(L.last_done, st));
+    {
+        NvtxRange wait("wait for product and result copy");
+        CK(cudaStreamSynchronize(st));
+    }
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    cudaEventElapsedTime(&ms, L.ev0, L.ev1);
     t_stats.path = use_fft ? 2 : (blocked ? 3 : pl.path);
     t_stats.log2_n = use_fft ? fp.k : pl.k;
     t_stats.primes = use_fft ? 0 : pl.nprimes;
     t_stats.digit_bits = use_fft ? fp.b : (set_wide(pl.set) ? 64 : 32);
     t_stats.device_ms = ms;
-    t_stats.fft_max_distance = use_fft ? *c.h_maxdist : 0.0;
+    t_stats.fft_max_distance = use_fft ? *L.h_maxdist : 0.0;
     if (fft_failed) return PREC_GPU_E_FFT_ROUNDING;
     if (total > lout) memset(out + lout, 0, (total - lout) * sizeof(uint64_t));
-    if (*c.h_err & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
-    if (*c.h_err) return PREC_GPU_E_INTERNAL;
+    if (*L.h_err & kDevErrTimeout) return PREC_GPU_E_TIMEOUT;
+    if (*L.h_err) return PREC_GPU_E_INTERNAL;
     return 0;
 }
 
@@ -939,49 +1047,22 @@ void prec_gpu_shutdown(void) {
     std::lock_guard<std::mutex> lk(c.mu);
     if (!c.ready) return;
     cudaDeviceSynchronize();
-    cudaFree(c.ws);
-    cudaFree(c.io);
+    for (auto& L : c.lanes) {
+        std::lock_guard<std::mutex> ll(L->mu);
+        lane_destroy(*L);
+    }
+    c.lanes.clear();
+    c.gen.fetch_add(1, std::memory_order_relaxed);  // every thread takes a new lane next time
     cudaFree(c.tables);
     cudaFree(c.fft_tw);
-    cudaFree(c.fft_args);
-    c.fft_args = nullptr;
-    fft_release_graphs();
     cudaFree(c.d_err);
     cudaFreeHost(c.h_err);
-    cudaEventDestroy(c.last_done);
-    cudaEventDestroy(c.ev0);
-    cudaEventDestroy(c.ev1);
-    cudaEventDestroy(c.ev_a);
-    cudaEventDestroy(c.ev_b);
-    for (int i = 0; i <= kMaxStages; ++i) cudaEventDestroy(c.stage_ev[i]);
-    for (int p = 0; p < kMaxPrimes; ++p) {
-        cudaStreamDestroy(c.prime_streams.s[p]);
-        cudaEventDestroy(c.prime_streams.join[p]);
-    }
-    cudaEventDestroy(c.prime_streams.fork);
-    c.prime_streams = PrimeStreams{};
-    for (auto& kv : c.graphs) {
-        cudaGraphExecDestroy(kv.second.exec);
-        cudaGraphDestroy(kv.second.graph);
-        cudaFree(kv.second.d_desc);
-    }
-    c.graphs.clear();
-    cudaStreamDestroy(c.cap);
-    c.cap = nullptr;
-    cudaStreamDestroy(c.copy);
-    c.copy = nullptr;
-    for (int i = 0; i < kCrtMaxChunks; ++i) cudaEventDestroy(c.chunk_done[i]);
-    cudaEventDestroy(c.copy_done);
-    cudaFree(c.chunk_words);
-    c.chunk_words = nullptr;
     if (c.pool) cudaMemPoolDestroy(c.pool);
     c.pool = nullptr;
-    cudaStreamDestroy(c.stream);
-    c.ws = nullptr;
-    c.io = nullptr;
     c.tables = nullptr;
-    c.ws_cap = c.io_cap = 0;
-    c.ready = false;
+    c.fft_tw = nullptr;
+    c.d_err = c.h_err = nullptr;
+    c.ready.store(false, std::memory_order_release);
 }
 
 int prec_gpu_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, uint64_t* out) {
@@ -1008,24 +1089,27 @@ int prec_gpu_mul_device(const uint64_t* d_a, size_t an, const uint64_t* d_b, siz
                         void* stream) {
     if (!d_a || !d_b || !d_out || an == 0 || bn == 0) return PREC_GPU_E_ARG;
     Ctx& c = g_ctx;
-    std::lock_guard<std::mutex> lk(c.mu);
-    int r = init_locked(c, -1);
+    Lane* lp = nullptr;
+    int r = thread_lane(c, lp);
     if (r) return r;
+    Lane& L = *lp;
+    std::lock_guard<std::mutex> lk(L.mu);
+    NvtxRange range("prec_gpu_mul_device %zux%zu", an, bn);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Plan pl;
     const uint64_t B = block_limbs();
     if (an > B || bn > B) {
-        if ((r = prepare_blocked(c, an, bn, B, pl))) return r;
-        CK(cudaStreamWaitEvent(st, c.last_done, 0));
-        if ((r = enqueue_blocked(c, d_a, an, d_b, bn, d_out, st, B))) return r;
-        CK(cudaEventRecord(c.last_done, st));
+        if ((r = prepare_blocked(L, an, bn, B, pl))) return r;
+        CK(cudaStreamWaitEvent(st, L.last_done, 0));
+        if ((r = enqueue_blocked(c, L, d_a, an, d_b, bn, d_out, st, B, c.d_err))) return r;
+        CK(cudaEventRecord(L.last_done, st));
         return 0;
     }
     if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits()))) return r;
-    if ((r = ensure_ws(c, pl.work_bytes))) return r;
-    CK(cudaStreamWaitEvent(st, c.last_done, 0));
-    if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st))) return r;
-    CK(cudaEventRecord(c.last_done, st));
+    if ((r = ensure_ws(L, pl.work_bytes))) return r;
+    CK(cudaStreamWaitEvent(st, L.last_done, 0));
+    if ((r = enqueue_ntt(c, L, d_a, an, d_b, bn, d_out, pl, st, c.d_err))) return r;
+    CK(cudaEventRecord(L.last_done, st));
     return 0;
 }
 
@@ -1033,19 +1117,21 @@ int prec_gpu_mul_device_profile(const uint64_t* d_a, size_t an, const uint64_t* 
                                 uint64_t* d_out, void* stream, float* stage_ms, int* nstages) {
     if (!d_a || !d_b || !d_out || an == 0 || bn == 0 || !stage_ms || !nstages) return PREC_GPU_E_ARG;
     Ctx& c = g_ctx;
-    std::lock_guard<std::mutex> lk(c.mu);
-    int r = init_locked(c, -1);
+    Lane* lp = nullptr;
+    int r = thread_lane(c, lp);
     if (r) return r;
+    Lane& L = *lp;
+    std::lock_guard<std::mutex> lk(L.mu);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Plan pl;
     if ((r = plan_for(2 * (uint64_t)an, 2 * (uint64_t)bn, an + bn, pl, wide_digits()))) return r;
-    if ((r = ensure_ws(c, pl.work_bytes))) return r;
-    CK(cudaStreamWaitEvent(st, c.last_done, 0));
-    if ((r = enqueue_ntt(c, d_a, an, d_b, bn, d_out, pl, st, c.stage_ev))) return r;
-    CK(cudaEventRecord(c.last_done, st));
+    if ((r = ensure_ws(L, pl.work_bytes))) return r;
+    CK(cudaStreamWaitEvent(st, L.last_done, 0));
+    if ((r = enqueue_ntt(c, L, d_a, an, d_b, bn, d_out, pl, st, c.d_err, L.stage_ev))) return r;
+    CK(cudaEventRecord(L.last_done, st));
     CK(cudaStreamSynchronize(st));
     const int n = kStageCount[pl.path];
-    for (int i = 0; i < n; ++i) CK(cudaEventElapsedTime(&stage_ms[i], c.stage_ev[i], c.stage_ev[i + 1]));
+    for (int i = 0; i < n; ++i) CK(cudaEventElapsedTime(&stage_ms[i], L.stage_ev[i], L.stage_ev[i + 1]));
     *nstages = n;
     return 0;
 }

@@ -4,13 +4,34 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
+#include <cstdarg>
 #include <cstddef>
 #include <cstdint>
+#include <cstdio>
 #include <mutex>
 
 #include "ntt_kernels.cuh"
 
 namespace precgpu {
+
+// A named NVTX range for the scope (header-only NVTX: without a profiler
+// attached a push/pop costs a few nanoseconds).  Nsight Systems shows the
+// library's host calls and their phases on the calling thread's row.
+struct NvtxRange {
+    explicit NvtxRange(const char* fmt, ...) {
+        char buf[96];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        nvtxRangePushA(buf);
+    }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // transform plan of one product on the NTT band
 struct Plan {

@@ -87,6 +87,7 @@ static size_t footprint(const Plan& pl) { return pl.path == 1 ? pl.work_bytes : 
 // launches one admitted request on its slot (worker thread, lock not held)
 static int launch_request(prec_gpu_server* s, Slot& sl) {
     const Request& r = sl.req;
+    NvtxRange range("serve request %llu: %zux%zu", (unsigned long long)r.ticket, r.p.an, r.p.bn);
     cudaStream_t st = sl.stream;
     const prec_gpu_product_t& p = r.p;
     const size_t si = (size_t)(&sl - s->slots.data());

@@ -265,9 +265,49 @@ def test_invalid_arguments(gpu):
     assert not out[:8].any()
 
 
+def test_device_calls_from_threads_on_own_streams(gpu):
+    """Device-pointer products from four threads, each on its own stream
+    (each thread has its own library workspace, so the products may run at
+    the same time), across both digit widths and a square: all exact."""
+    import threading
+    torch = pytest.importorskip("torch")
+    shapes = [(300000, 200000), (8192, 8192), (70000, 70000), (1 << 19, 1 << 19)]
+    cases = []
+    for i, (an, bn) in enumerate(shapes):
+        a = O.splitmix64(60 + i, an)
+        b = a if i == 2 else O.splitmix64(70 + i, bn)
+        cases.append((a, b, O.mul_ntt(a, b)))
+    errors = []
+
+    def work(t):
+        try:
+            a, b, want = cases[t]
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                ta = torch.from_numpy(a.view(np.int64)).cuda()
+                tb = ta if b is a else torch.from_numpy(b.view(np.int64)).cuda()
+                out = torch.empty(len(a) + len(b), dtype=torch.int64, device="cuda")
+                for _ in range(3):
+                    gpu.check(gpu.lib().prec_gpu_mul_device(ta.data_ptr(), len(a), tb.data_ptr(), len(b),
+                                                            out.data_ptr(), s.cuda_stream))
+                gpu.stream_check(s.cuda_stream)
+                if not np.array_equal(out.cpu().numpy().view(np.uint64), want):
+                    errors.append(t)
+        except Exception as e:  # pragma: no cover - reported below
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(len(cases))]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert not errors, errors
+
+
 def test_host_calls_from_many_threads(gpu):
-    """Host-pointer calls are serialised on one context: products from eight
-    threads at once, across both bands and squares, are all exact."""
+    """Host-pointer calls from eight threads at once (each thread with its own
+    stream and workspace, running concurrently), across both bands and
+    squares, are all exact."""
     import threading
     shapes = [(20000, 15000), (3000, 2999), (200, 300), (65536, 65536), (9000, 9000), (1, 7), (6144, 6144),
               (100000, 1000)]

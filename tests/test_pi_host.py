@@ -21,17 +21,31 @@ SRC = [os.path.join(ROOT, "tests", "pi_host", "bignum_check.cpp"),
        os.path.join(ROOT, "preclib_gb300", "pi", "bignum.cpp")]
 
 
-@pytest.fixture(scope="module")
-def run(tmp_path_factory):
+SANITIZE = ["-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-fno-omit-frame-pointer", "-g"]
+
+
+@pytest.fixture(scope="module", params=["plain", "sanitized"])
+def run(request, tmp_path_factory):
+    """The check program, plain and built with AddressSanitizer and
+    UndefinedBehaviorSanitizer (any report fails the run: out-of-bounds or
+    use-after-free on the limb buffers, leaks, signed overflow, shifts past
+    the width)."""
     if not shutil.which("g++"):
         pytest.skip("no g++")
     exe = str(tmp_path_factory.mktemp("bignum") / "bignum_check")
-    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-DPI_LEAF_DIGITS=64", "-o", exe] + SRC,
-                   check=True, capture_output=True, text=True)
+    flags = SANITIZE if request.param == "sanitized" else []
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-DPI_LEAF_DIGITS=64", *flags, "-o", exe] + SRC,
+                       capture_output=True, text=True)
+    if r.returncode and request.param == "sanitized":
+        pytest.skip("no sanitizer runtime: " + r.stderr[-200:])
+    assert r.returncode == 0, r.stderr
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
 
     def go(lines):
-        r = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=300)
-        assert r.returncode == 0, r.stderr
+        r = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=600,
+                           env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        assert "runtime error" not in r.stderr and "Sanitizer" not in r.stderr, r.stderr[-2000:]
         return r.stdout.split("\n")[:len(lines)]
     return go
 

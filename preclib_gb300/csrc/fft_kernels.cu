@@ -496,13 +496,13 @@ static int carry_blocks(uint64_t b, uint64_t ncoef, uint64_t lout) {
 static void launch4(const FftArgs& f, FftArgs* d_args, int nblk, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], st);
     const int ncol = (1 << f.k2) / kFftCols;
-    k_fft_fwd_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(f, d_args);
+    launch_kernel(k_fft_fwd_cols<kFftCols>, ncol, 256, cols_smem(f.k1), st, f, d_args);
     if (ev) cudaEventRecord(ev[1], st);
-    k_fft_rows<<<(1 << f.k1) / 2 + 1, 256, rows_smem(f.k2), st>>>(d_args);
+    launch_kernel(k_fft_rows, (1 << f.k1) / 2 + 1, 256, rows_smem(f.k2), st, d_args);
     if (ev) cudaEventRecord(ev[2], st);
-    k_fft_inv_cols<kFftCols><<<ncol, 256, cols_smem(f.k1), st>>>(d_args);
+    launch_kernel(k_fft_inv_cols<kFftCols>, ncol, 256, cols_smem(f.k1), st, d_args);
     if (ev) cudaEventRecord(ev[3], st);
-    k_fft_carry<<<nblk, kFftCarryThreads, 0, st>>>(d_args);
+    launch_kernel(k_fft_carry, nblk, kFftCarryThreads, 0, st, d_args);
     count_launches(4);
     if (ev) cudaEventRecord(ev[4], st);
 }
@@ -550,28 +550,21 @@ int fft_launch(const FftArgs& f, FftArgs* d_args, cudaStream_t st, cudaEvent_t* 
         it = g_fft_graphs.find(key);
     }
     if (it == g_fft_graphs.end()) {
-        if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return (int)e;
+        // the four launches as a chain of kernel nodes (explicit
+        // construction: no stream capture)
+        GraphRecorder rec;
+        if ((e = cudaGraphCreate(&rec.graph, 0)) != cudaSuccess) return (int)e;
         const uint64_t before = launches_this_thread();
+        thread_recorder() = &rec;
         launch4(f, d_args, carry_blocks(16, 1ull << (f.k1 + f.k2), 0), cap, nullptr);
-        uncount_launches(launches_this_thread() - before);  // captured: counted at every replay
-        cudaGraph_t g = nullptr;
-        e = cudaStreamEndCapture(cap, &g);
+        thread_recorder() = nullptr;
+        uncount_launches(launches_this_thread() - before);  // recorded: counted at every replay
+        cudaGraph_t g = rec.graph;
+        e = rec.err;
         FftGraph fg;
-        // the forward column node: the one whose kernel is k_fft_fwd_cols
-        size_t n = 0;
-        if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &n);
-        std::vector<cudaGraphNode_t> nodes(n);
-        if (e == cudaSuccess && n) e = cudaGraphGetNodes(g, nodes.data(), &n);
-        for (size_t i = 0; e == cudaSuccess && i < n && !fg.first; ++i) {
-            cudaGraphNodeType t;
-            if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
-            cudaKernelNodeParams kp{};
-            if (cudaGraphKernelNodeGetParams(nodes[i], &kp) != cudaSuccess) continue;
-            if (kp.func == (void*)k_fft_fwd_cols<kFftCols>) {
-                fg.first = nodes[i];
-                fg.params = kp;
-            }
-        }
+        // the forward column node: the first recorded
+        fg.first = rec.first;
+        if (e == cudaSuccess && fg.first) e = cudaGraphKernelNodeGetParams(fg.first, &fg.params);
         if (e == cudaSuccess && !fg.first) e = cudaErrorInvalidValue;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&fg.exec, g, 0);
         if (e != cudaSuccess) {

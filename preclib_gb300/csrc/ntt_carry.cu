@@ -289,10 +289,10 @@ __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, cons
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int max_nblk,
                       int nblk_launch) {
     const dim3 grid(batch ? max_nblk : (nblk_launch > 0 ? nblk_launch : a.nblk), 1, count);
-    if (set == 0) k_crt_carry<0><<<grid, kCarryThreads, 0, st>>>(a, batch);
-    else if (set == 1) k_crt_carry<1><<<grid, kCarryThreads, 0, st>>>(a, batch);
-    else if (set == kWideSet) k_crt_carry<kWideSet><<<grid, kCarryThreads, 0, st>>>(a, batch);
-    else k_crt_carry<kWideSetL><<<grid, kCarryThreads, 0, st>>>(a, batch);
+    if (set == 0) launch_kernel(k_crt_carry<0>, grid, kCarryThreads, 0, st, a, batch);
+    else if (set == 1) launch_kernel(k_crt_carry<1>, grid, kCarryThreads, 0, st, a, batch);
+    else if (set == kWideSet) launch_kernel(k_crt_carry<kWideSet>, grid, kCarryThreads, 0, st, a, batch);
+    else launch_kernel(k_crt_carry<kWideSetL>, grid, kCarryThreads, 0, st, a, batch);
     count_launches(1);
 }
 

@@ -12,7 +12,7 @@ void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
     const size_t smem = col_smem(a.k1, cg);
 #define X(S, MM, CC, RR)                                                     \
     if (set == S && a.k1 == MM && cg == CC && mr == RR) {                     \
-        k_fwd_cols<S, MM, CC, RR><<<grid, 32 * CC, smem, st>>>(a, batch);     \
+        launch_kernel(k_fwd_cols<S, MM, CC, RR>, grid, 32 * CC, smem, st, a, batch); \
         count_launches(1);                                                  \
         return;                                                             \
     }

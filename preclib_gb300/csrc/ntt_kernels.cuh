@@ -2,6 +2,9 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <tuple>
+#include <utility>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -131,9 +134,52 @@ constexpr int kCarryThreads = 256;
 constexpr int kCarryLimbs = PREC_CARRY_LIMBS;  // limbs per thread in the carry kernel
 constexpr int kColGroup = PREC_COL_GROUP;      // adjacent columns per column-pass CTA (4 when N1 = 2^13)
 
+// Explicit graph construction.  While a thread has a recorder installed,
+// the library's launchers (launch_kernel) add kernel nodes to the
+// recorder's graph instead of launching: a node depends on the node last
+// recorded for the same stream handle, or on the recorder's fork point for
+// that stream.  The library's graphs are built this way rather than by
+// stream capture: a capture in progress can be broken by a device-wide
+// synchronising call (cudaFree, cudaDeviceSynchronize, ...) that another
+// thread of the process makes at the same time, and callers and lanes run
+// products from several threads.
+struct GraphRecorder {
+    cudaGraph_t graph = nullptr;
+    std::vector<std::pair<cudaStream_t, cudaGraphNode_t>> last;  // per stream handle
+    cudaGraphNode_t first = nullptr;  // the first node recorded
+    cudaError_t err = cudaSuccess;
+    uint64_t nodes = 0;
+    cudaGraphNode_t tail(cudaStream_t st) const;
+    void set_tail(cudaStream_t st, cudaGraphNode_t n);
+    // `to` starts after what is recorded on `from` so far (a fork)
+    void fork(cudaStream_t from, cudaStream_t to) { set_tail(to, tail(from)); }
+    void add_kernel(const void* func, dim3 grid, dim3 block, size_t smem, void** args, cudaStream_t st);
+    void add_memset(void* dst, size_t bytes, cudaStream_t st);  // zero fill
+};
+// the calling thread's recorder (null: launchers launch)
+GraphRecorder*& thread_recorder();
+
+template <class Tuple, size_t... I>
+inline void arg_ptrs(Tuple& t, void** p, std::index_sequence<I...>) {
+    ((p[I] = static_cast<void*>(&std::get<I>(t))), ...);
+}
+
+// k<<<grid, block, smem, st>>>(args...), or a node of the thread's recorder
+template <class... P, class... A>
+inline void launch_kernel(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
+    if (GraphRecorder* r = thread_recorder()) {
+        std::tuple<P...> vals(std::forward<A>(args)...);
+        void* ptrs[sizeof...(P) > 0 ? sizeof...(P) : 1];
+        arg_ptrs(vals, ptrs, std::index_sequence_for<P...>{});
+        r->add_kernel(reinterpret_cast<const void*>(k), grid, block, smem, ptrs, st);
+    } else {
+        k<<<grid, block, smem, st>>>(std::forward<A>(args)...);
+    }
+}
+
 // Kernel launches issued by the library (process-wide, prec_gpu_launch_count);
 // every launcher adds its launches.  launches_this_thread() lets a graph
-// capture take back the launches it only recorded.
+// recording take back the launches it only recorded.
 void count_launches(uint64_t n);
 uint64_t launches_this_thread();
 void uncount_launches(uint64_t n);

@@ -158,7 +158,7 @@ void launch_rows(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* ba
     const int mr = row_radix_cap(m, a.rmr);
 #define X(S, MM, SQ, RR)                                                                  \
     if (set == S && m == MM && (a.square != 0) == SQ && mr == RR) {                       \
-        k_rows<S, MM, SQ, RR><<<grid, threads, smem, st>>>(a, batch);                     \
+        launch_kernel(k_rows<S, MM, SQ, RR>, grid, threads, smem, st, a, batch);                 \
         count_launches(1);                                                              \
         return;                                                                         \
     }

@@ -164,7 +164,7 @@ void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int cou
     const size_t smem = ntt_small_smem_bytes(k);
 #define X(MM) \
     if (k == MM) {                                                     \
-        k_small<MM><<<count, threads, smem, st>>>(d_descs, one, f);   \
+        launch_kernel(k_small<MM>, count, threads, smem, st, d_descs, one, f); \
         count_launches(1);                                             \
     }
     PREC_SMALL(X)

@@ -104,16 +104,21 @@ static void batch_free(prec_gpu_batch* b) {
     } while (0)
 
 // all of the batch's device work, enqueued on the class streams (forked
-// from and joined to `origin`), or on `origin` alone when `branch` is false
+// from and joined to `origin`), or on `origin` alone when `branch` is false.
+// With a graph recorder installed on the thread, the same work becomes
+// nodes: one independent chain per class stream, the zero fills on `origin`.
 static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
-    if (branch) cudaEventRecord(b->fork, origin);
+    GraphRecorder* rec = thread_recorder();
+    if (branch && !rec) cudaEventRecord(b->fork, origin);
     for (int i : b->zero_items) {
         const prec_gpu_product_t& p = b->items[i];
-        if (p.an + p.bn) cudaMemsetAsync(p.out, 0, (p.an + p.bn) * sizeof(uint64_t), origin);
+        if (!(p.an + p.bn)) continue;
+        if (rec) rec->add_memset(p.out, (p.an + p.bn) * sizeof(uint64_t), origin);
+        else cudaMemsetAsync(p.out, 0, (p.an + p.bn) * sizeof(uint64_t), origin);
     }
     for (Cls& c : b->classes) {
         cudaStream_t st = branch ? c.stream : origin;
-        if (branch) cudaStreamWaitEvent(st, b->fork, 0);
+        if (branch && !rec) cudaStreamWaitEvent(st, b->fork, 0);
         if (c.pl.path == 0) {
             ntt_launch_small(c.d_small, nullptr, (int)c.items.size(), c.k, ctx_field(0), st);
         } else {
@@ -133,7 +138,7 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
             for (const Chunk& ch : c.chunks)
                 ntt_launch_4step_batch(c.pl.set, args, c.d_ptrs + ch.first, ch.count, ch.max_nblk, st);
         }
-        if (branch) {
+        if (branch && !rec) {
             cudaEventRecord(c.join, st);
             cudaStreamWaitEvent(origin, c.join, 0);
         }
@@ -302,15 +307,20 @@ int prec_gpu_batch_run(prec_gpu_batch_t* b, void* stream) {
     NvtxRange range("prec_gpu_batch_run %zu products, %zu classes", b->items.size(), b->classes.size());
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (!b->exec) {
-        cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+        // the graph built node by node (no stream capture: another thread's
+        // device-wide synchronising call cannot break it)
+        GraphRecorder rec;
+        cudaError_t e = cudaGraphCreate(&rec.graph, 0);
         if (e != cudaSuccess) return cuda_code(e);
         const uint64_t before = launches_this_thread();
+        thread_recorder() = &rec;
         batch_enqueue(b, b->cap, true);
-        // captured, not launched: counted at every replay instead
+        thread_recorder() = nullptr;
+        // recorded, not launched: counted at every replay instead
         b->graph_launches = launches_this_thread() - before;
         uncount_launches(b->graph_launches);
-        e = cudaStreamEndCapture(b->cap, &b->graph);
-        if (e != cudaSuccess) return cuda_code(e);
+        b->graph = rec.graph;
+        if (rec.err != cudaSuccess) return cuda_code(rec.err);
         e = cudaGraphInstantiate(&b->exec, b->graph, 0);
         if (e != cudaSuccess) return cuda_code(e);
     }

@@ -338,6 +338,58 @@ bool wide_digits() {
 
 static Ctx g_ctx;
 
+static thread_local GraphRecorder* t_recorder = nullptr;
+GraphRecorder*& thread_recorder() { return t_recorder; }
+
+cudaGraphNode_t GraphRecorder::tail(cudaStream_t st) const {
+    for (const auto& p : last)
+        if (p.first == st) return p.second;
+    return nullptr;
+}
+
+void GraphRecorder::set_tail(cudaStream_t st, cudaGraphNode_t n) {
+    for (auto& p : last)
+        if (p.first == st) {
+            p.second = n;
+            return;
+        }
+    last.emplace_back(st, n);
+}
+
+void GraphRecorder::add_kernel(const void* func, dim3 grid, dim3 block, size_t smem, void** args, cudaStream_t st) {
+    if (err != cudaSuccess) return;
+    cudaKernelNodeParams kp{};
+    kp.func = const_cast<void*>(func);
+    kp.gridDim = grid;
+    kp.blockDim = block;
+    kp.sharedMemBytes = (unsigned)smem;
+    kp.kernelParams = args;  // the values are copied into the node
+    kp.extra = nullptr;
+    cudaGraphNode_t dep = tail(st), node = nullptr;
+    err = cudaGraphAddKernelNode(&node, graph, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+    if (err != cudaSuccess) return;
+    if (!first) first = node;
+    set_tail(st, node);
+    ++nodes;
+}
+
+void GraphRecorder::add_memset(void* dst, size_t bytes, cudaStream_t st) {
+    if (err != cudaSuccess || bytes == 0) return;
+    cudaMemsetParams mp{};
+    mp.dst = dst;
+    mp.value = 0;
+    mp.elementSize = 1;
+    mp.width = bytes;
+    mp.height = 1;
+    mp.pitch = 0;
+    cudaGraphNode_t dep = tail(st), node = nullptr;
+    err = cudaGraphAddMemsetNode(&node, graph, dep ? &dep : nullptr, dep ? 1 : 0, &mp);
+    if (err != cudaSuccess) return;
+    if (!first) first = node;
+    set_tail(st, node);
+    ++nodes;
+}
+
 static std::atomic<uint64_t> g_launches{0};
 static thread_local uint64_t t_launches = 0;
 
@@ -359,10 +411,21 @@ int cuda_code(cudaError_t e) {
     return PREC_GPU_E_CUDA;
 }
 
-#define CK(x)                                  \
-    do {                                       \
-        cudaError_t _e = (x);                  \
-        if (_e != cudaSuccess) return cuda_code(_e); \
+// PREC_GPU_DEBUG=1: every failed CUDA call the library checks is named on
+// stderr with its error (file:line), before the code is returned
+static int cuda_fail(cudaError_t e, const char* call, const char* file, int line) {
+    static const bool debug = [] {
+        const char* s = std::getenv("PREC_GPU_DEBUG");
+        return s && s[0] == '1';
+    }();
+    if (debug) std::fprintf(stderr, "prec_gpu: %s:%d: %s: %s\n", file, line, call, cudaGetErrorName(e));
+    return cuda_code(e);
+}
+
+#define CK(x)                                                                \
+    do {                                                                     \
+        cudaError_t _e = (x);                                                \
+        if (_e != cudaSuccess) return cuda_fail(_e, #x, __FILE__, __LINE__); \
     } while (0)
 
 // Per set and prime: Shoup tables of the sub-transform roots (forward and
@@ -652,25 +715,27 @@ static int enqueue_graph(Lane& L, const ProdArgs& args, const Plan& pl, cudaStre
         const uint64_t lout_max = set_wide(pl.set) ? (1ull << pl.k) + 1 : (1ull << pl.k) / 2 + 1;
         const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
         const int max_nblk = (int)((lout_max + bl - 1) / bl);
-        cudaError_t err = cudaStreamBeginCapture(L.cap, cudaStreamCaptureModeThreadLocal);
+        // the four launches as a chain of kernel nodes (explicit
+        // construction: no stream capture)
+        GraphRecorder rec;
+        cudaError_t err = cudaGraphCreate(&rec.graph, 0);
         if (err != cudaSuccess) {
             cudaFree(e.d_desc);
             return cuda_code(err);
         }
         const uint64_t before = launches_this_thread();
+        t_recorder = &rec;
         launch_fwd_cols(pl.set, first, L.cap);
         launch_rows(pl.set, cls, L.cap, e.d_desc, 1);
         launch_inv_cols(pl.set, cls, L.cap, e.d_desc, 1);
         launch_crt_carry(pl.set, cls, L.cap, e.d_desc, 1, max_nblk);
-        e.launches = launches_this_thread() - before;  // captured, counted at every replay
+        t_recorder = nullptr;
+        e.launches = launches_this_thread() - before;  // recorded, counted at every replay
         uncount_launches(e.launches);
-        cudaGraph_t g = nullptr;
-        err = cudaStreamEndCapture(L.cap, &g);
-        // the forward column node: the graph's only node without a dependency
-        size_t n = 0;
-        if (err == cudaSuccess) err = cudaGraphGetRootNodes(g, nullptr, &n);
-        cudaGraphNode_t root = nullptr;
-        if (err == cudaSuccess && n == 1) err = cudaGraphGetRootNodes(g, &root, &n);
+        cudaGraph_t g = rec.graph;
+        err = rec.err;
+        // the forward column node: the first recorded
+        cudaGraphNode_t root = rec.first;
         if (err == cudaSuccess && root) err = cudaGraphKernelNodeGetParams(root, &e.params);
         if (err == cudaSuccess && !root) err = cudaErrorInvalidValue;
         e.first = root;

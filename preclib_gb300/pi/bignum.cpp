@@ -343,7 +343,7 @@ void divmod_recip(const Nat& N, const Nat& D, const Nat& X, size_t P, Nat& q, Na
 // ---------------------------------------------------------------------------
 
 // Y with |Y - 2^(e/2 + p) / sqrt(n)| <= 4, for even e >= bitlen(n)
-static Nat invsqrt(const Nat& n, size_t e, size_t p) {
+Nat invsqrt(const Nat& n, size_t e, size_t p) {
     const size_t L = bitlen(n);
     if (p <= 40) {
         const size_t sh = L > 56 ? ((L - 56 + 1) & ~(size_t)1) : 0;  // even shift

@@ -108,6 +108,9 @@ void divmod(const Nat& N, const Nat& D, Nat& q, Nat& r);
 void divmod_recip(const Nat& N, const Nat& D, const Nat& X, size_t P, Nat& q, Nat& r);
 // floor(sqrt(n))
 Nat isqrt(const Nat& n);
+// Y with |Y - 2^(e/2 + p) / sqrt(n)| <= 4, for even e >= bitlen(n)
+// (the Newton inverse square root isqrt is built on)
+Nat invsqrt(const Nat& n, size_t e, size_t p);
 
 // The powers 10^(L * 2^j), j < levels (L = the leaf size in digits), and
 // their reciprocals: all that decimal conversion needs besides x, so a

@@ -12,9 +12,14 @@
 //     level needs it) are independent and go to the GPU as one batch
 //     (prec_gpu_mul_batch); the node values are shape independent
 //     (T(a,b) = sum_k t_k P(a,k) Q(k+1,b)), so any tree gives the same Q, T;
-//   * the square root, the final division and the decimal conversion run
-//     Newton iterations whose products go to the GPU (bignum.cpp), the
-//     conversion's splits once more as one batch per level;
+//   * the square root and the final division run their Newton iterations
+//     on numbers resident in device memory (dnat.cu): products through
+//     prec_gpu_mul_device, shifts, additions and comparisons as device
+//     kernels, only the operands in and the quotient out crossing the link
+//     (PI_GB300_HOST_NEWTON=1: the host-resident iterations of bignum.cpp,
+//     every product staged through host memory, for comparison);
+//   * the decimal conversion runs Newton divisions whose products go to the
+//     GPU (bignum.cpp), its splits as one batch per level;
 //   * the square root and the conversion's powers of ten (with their
 //     reciprocals) depend only on the digit count, so a second host thread
 //     computes them while the binary splitting and the division run.
@@ -48,6 +53,7 @@
 
 #include "../../include/prec_gpu.h"
 #include "bignum.hpp"
+#include "dnat.hpp"
 #include "pi_device.hpp"
 
 using namespace precpi;
@@ -84,6 +90,18 @@ void check_cuda(cudaError_t e, const char* what) {
 // multiply backend on libprecgpu
 // ---------------------------------------------------------------------------
 
+// device-math work of the Newton steps (summary line of --phases)
+static std::mutex g_dm_mu;
+static size_t g_dm_products = 0, g_dm_syncs = 0;
+static void dm_stats_add(const DevMath& dm) {
+    std::lock_guard<std::mutex> lk(g_dm_mu);
+    g_dm_products += dm.products;
+    g_dm_syncs += dm.syncs;
+}
+
+static cudaStream_t g_stream = nullptr;  // the main thread's stream (the backend's)
+static cudaStream_t gpu_stream() { return g_stream; }
+
 struct GpuBackend : MulBackend {
     cudaStream_t st = nullptr;
     u64* h_buf = nullptr;  // pinned staging of a batch (operands, then results)
@@ -97,7 +115,10 @@ struct GpuBackend : MulBackend {
     size_t gpu_products = 0, host_products = 0, batches = 0;
     double mul_seconds = 0.0;  // wall time inside single products (host API), summed over threads
 
-    GpuBackend() { check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream"); }
+    GpuBackend() {
+        check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+        g_stream = st;
+    }
     ~GpuBackend() override {
         if (h_buf) cudaFreeHost(h_buf);
         if (d_buf) cudaFree(d_buf);
@@ -665,7 +686,10 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
     // conversion do not depend on the series: a second thread computes them
     // while this one runs the binary splitting and the division (the
     // reference program computes the same values in sequence)
-    Nat root;
+    const char* hn = std::getenv("PI_GB300_HOST_NEWTON");
+    const bool host_newton = hn && hn[0] == '1';
+    Nat root;     // host-resident form
+    DNat root_d;  // device-resident form
     DecimalPowers pows;
     std::promise<void> root_set;
     std::future<void> root_ready = root_set.get_future();
@@ -673,7 +697,23 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
     const int levels = decimal_levels(digits + 2);
     std::thread side([&] {
         const double s0 = now_sec();
-        root = isqrt(mul_u64(pow_u64(10, 2 * work), 10005));
+        if (host_newton) {
+            root = isqrt(mul_u64(pow_u64(10, 2 * work), 10005));
+        } else {
+            // 10005 * 10^(2 work) and its square root without leaving the device
+            cudaStream_t sst = nullptr;
+            check_cuda(cudaStreamCreateWithFlags(&sst, cudaStreamNonBlocking), "stream");
+            {
+                DevMath dm(sst);
+                const DNat n = dm.mul_u64(dm.pow_u64(10, 2 * work), 10005);
+                root_d = dm.isqrt(n);
+                check_cuda(cudaStreamSynchronize(sst), "square root");
+                dm_stats_add(dm);
+            }
+            check_cuda(cudaStreamSynchronize(sst), "square root");
+            root_d.st = nullptr;  // handed to the main thread (its stream adopts it)
+            cudaStreamDestroy(sst);
+        }
         const double s1 = now_sec();
         root_set.set_value();
         pows = decimal_powers(levels);
@@ -696,13 +736,32 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
     const Nat q426880 = mul_u64(Q, 426880);
     const size_t root_bits = (size_t)(std::log2(std::sqrt(10005.0)) + (double)work * std::log2(10.0)) + 2;
     const size_t P = bitlen(q426880) + root_bits - bitlen(T) + 2 + 32;
-    const Nat X = recip(T, P);
-    const double t2r = now_sec();
-    root_ready.wait();
-    double t2 = now_sec();
-    const Nat num = mul(q426880, root);
     Nat pi, rem;
-    divmod_recip(num, T, X, P, pi, rem);
+    double t2r = 0, t2 = 0;
+    if (host_newton) {
+        const Nat X = recip(T, P);
+        t2r = now_sec();
+        root_ready.wait();
+        t2 = now_sec();
+        const Nat num = mul(q426880, root);
+        divmod_recip(num, T, X, P, pi, rem);
+    } else {
+        // T, Q * 426880 up, the quotient down; everything between on the device
+        DevMath dm(gpu_stream());
+        const DNat Td = dm.upload(T);
+        const DNat X = dm.recip(Td, P);
+        const DNat qd = dm.upload(q426880);
+        t2r = now_sec();
+        root_ready.wait();
+        t2 = now_sec();
+        dm.adopt(root_d);
+        const DNat num = dm.mul(qd, root_d);
+        root_d = DNat();
+        DNat pid, remd;
+        dm.divmod_recip(num, Td, X, P, &pid, &remd);
+        pi = dm.download(pid);
+        dm_stats_add(dm);
+    }
     divmod_u64(pi, 10000000000ull);
     double t3 = now_sec();
     side.join();
@@ -793,9 +852,10 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "to_decimal %.6f sec\n", ph.dec);
         std::fprintf(stderr, "gpu_products %zu host_products %zu gpu_batches %zu single-product time %.3f s\n",
                      be->gpu_products, be->host_products, be->batches, be->mul_seconds);
+        std::fprintf(stderr, "device_newton_products %zu device_newton_syncs %zu\n", g_dm_products, g_dm_syncs);
     }
     std::fprintf(stderr, "gpu_launches %llu\n",
-                 (unsigned long long)(prec_gpu_launch_count() + signed_add_launches()));
+                 (unsigned long long)(prec_gpu_launch_count() + signed_add_launches() + dnat_launches()));
     if (!file.empty()) std::fprintf(stderr, "wrote %s\n", file.c_str());
     std::fprintf(stderr, "time %.6f sec\n", sec);
     return 0;

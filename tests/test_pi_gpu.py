@@ -32,3 +32,15 @@ def test_pi_digits_match_reference(gpu, tmp_path, digits):
     assert len(data) == want["bytes"]
     assert hashlib.sha256(data).hexdigest() == want["sha256"]
     assert data.startswith(b"3.14159265")
+
+
+def test_pi_digits_host_newton(gpu, tmp_path):
+    """The host-resident Newton steps (every product staged through host
+    memory), kept for comparison, give the same digits."""
+    want = _runs()[1000000]
+    out = tmp_path / "pi.txt"
+    env = dict(os.environ, PI_GB300_HOST_NEWTON="1")
+    r = subprocess.run([EXE, "1000000", "--file", str(out)], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr
+    data = out.read_bytes()
+    assert hashlib.sha256(data).hexdigest() == want["sha256"]

@@ -194,7 +194,9 @@ int prec_gpu_mul_device_noalloc(const uint64_t *d_a, size_t an, const uint64_t *
  * Replaces: nothing one-to-one; the reference forms products one at a time
  * (operator*, src/mul_basic.cpp:278-284), including the independent
  * products of one binary-splitting level (pi/pi_chudnovsky.cpp:141-144).
- * All pointers are device pointers; out receives an+bn limbs. */
+ * All pointers are device pointers; out receives an+bn limbs.  The products
+ * run concurrently: no output may overlap an operand or another output of
+ * the same batch. */
 typedef struct prec_gpu_product {
     const uint64_t *a;
     size_t an;
@@ -210,8 +212,8 @@ typedef struct prec_gpu_batch prec_gpu_batch_t;
 int prec_gpu_batch_create(const prec_gpu_product_t *items, size_t count, prec_gpu_batch_t **batch);
 
 /* Computes every product of the batch on `stream` (asynchronous).  The first
- * call captures the work into a CUDA graph (one stream branch per length
- * class); later calls replay it, recomputing the products from the current
+ * call records the work into a CUDA graph, built node by node (one branch
+ * per length class); later calls replay it, recomputing the products from the current
  * contents of the same operand buffers.  Device-side failures are reported
  * by prec_gpu_stream_check. */
 int prec_gpu_batch_run(prec_gpu_batch_t *batch, void *stream);

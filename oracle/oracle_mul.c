@@ -172,10 +172,26 @@ static void orc_plan_free(orc_plan_t *p) {
     free(p->iv);
 }
 
+/* ntt_get_mod_plan (mul_ntt.cpp:182-191): one cached plan per prime and
+ * thread, rebuilt when the transform length changes */
+static const orc_plan_t *orc_get_plan(int idx, size_t n) {
+    static _Thread_local orc_plan_t plans[3];
+    static _Thread_local size_t sizes[3];
+    if (sizes[idx] != n) {
+        if (sizes[idx]) orc_plan_free(&plans[idx]);
+        orc_plan_init(&plans[idx], idx, n);
+        sizes[idx] = n;
+    }
+    return &plans[idx];
+}
+
 /* forward Gentleman-Sande DIF, natural in, bit-reversed out
  * (scalar path of mul_ntt.cpp:193-255) */
-static void orc_ntt_fwd(uint32_t *a, size_t n, const orc_plan_t *p) {
-    const uint32_t mod = p->c.mod;
+static void orc_ntt_fwd(uint32_t *restrict a, size_t n, const orc_plan_t *p) {
+    /* local copies: stores to a[] cannot alias them, so they stay in registers */
+    const orc_mont_t c = p->c;
+    const uint32_t *restrict fw = p->fw;
+    const uint32_t mod = c.mod;
     for (size_t len = n; len >= 2; len >>= 1) {
         size_t half = len >> 1;
         for (size_t i = 0; i < n; i += len) {
@@ -185,7 +201,7 @@ static void orc_ntt_fwd(uint32_t *a, size_t n, const orc_plan_t *p) {
                 if (s >= mod) s -= mod;
                 uint32_t d = u >= v ? u - v : u + mod - v;
                 a[i + j] = s;
-                a[i + j + half] = orc_mmul(&p->c, d, p->fw[half + j]);
+                a[i + j + half] = orc_mmul(&c, d, fw[half + j]);
             }
         }
     }
@@ -193,14 +209,16 @@ static void orc_ntt_fwd(uint32_t *a, size_t n, const orc_plan_t *p) {
 
 /* inverse Cooley-Tukey DIT, bit-reversed in, natural out, times n^{-1}
  * (scalar path of mul_ntt.cpp:257-329) */
-static void orc_ntt_inv(uint32_t *a, size_t n, const orc_plan_t *p) {
-    const uint32_t mod = p->c.mod;
+static void orc_ntt_inv(uint32_t *restrict a, size_t n, const orc_plan_t *p) {
+    const orc_mont_t c = p->c;
+    const uint32_t *restrict iv = p->iv;
+    const uint32_t mod = c.mod;
     for (size_t len = 2; len <= n; len <<= 1) {
         size_t half = len >> 1;
         for (size_t i = 0; i < n; i += len) {
             for (size_t j = 0; j < half; ++j) {
                 uint32_t u = a[i + j];
-                uint32_t v = orc_mmul(&p->c, a[i + j + half], p->iv[half + j]);
+                uint32_t v = orc_mmul(&c, a[i + j + half], iv[half + j]);
                 uint32_t s = u + v;
                 if (s >= mod) s -= mod;
                 uint32_t d = u >= v ? u - v : u + mod - v;
@@ -209,7 +227,8 @@ static void orc_ntt_inv(uint32_t *a, size_t n, const orc_plan_t *p) {
             }
         }
     }
-    for (size_t i = 0; i < n; ++i) a[i] = orc_mmul(&p->c, a[i], p->inv_n);
+    const uint32_t inv_n = p->inv_n;
+    for (size_t i = 0; i < n; ++i) a[i] = orc_mmul(&c, a[i], inv_n);
 }
 
 /* ntt_digits (mul_ntt.cpp:331-342): limbs -> 16-bit digits, LSB first,
@@ -231,18 +250,17 @@ static size_t orc_digits16(const uint64_t *a, size_t an, uint32_t *d) {
 static void orc_convolve(const uint32_t *da, size_t na, const uint32_t *db,
                          size_t nb, size_t n, int idx, uint32_t *out,
                          uint32_t *scratch) {
-    orc_plan_t p;
-    orc_plan_init(&p, idx, n);
+    const orc_plan_t *p = orc_get_plan(idx, n);
+    const orc_mont_t c = p->c;
     memset(out, 0, n * sizeof(uint32_t));
     memset(scratch, 0, n * sizeof(uint32_t));
-    for (size_t i = 0; i < na; ++i) out[i] = orc_to_mont(&p.c, da[i]);
-    for (size_t i = 0; i < nb; ++i) scratch[i] = orc_to_mont(&p.c, db[i]);
-    orc_ntt_fwd(out, n, &p);
-    orc_ntt_fwd(scratch, n, &p);
-    for (size_t i = 0; i < n; ++i) out[i] = orc_mmul(&p.c, out[i], scratch[i]);
-    orc_ntt_inv(out, n, &p);
-    for (size_t i = 0; i < n; ++i) out[i] = orc_redc(&p.c, out[i]);
-    orc_plan_free(&p);
+    for (size_t i = 0; i < na; ++i) out[i] = orc_to_mont(&c, da[i]);
+    for (size_t i = 0; i < nb; ++i) scratch[i] = orc_to_mont(&c, db[i]);
+    orc_ntt_fwd(out, n, p);
+    orc_ntt_fwd(scratch, n, p);
+    for (size_t i = 0; i < n; ++i) out[i] = orc_mmul(&c, out[i], scratch[i]);
+    orc_ntt_inv(out, n, p);
+    for (size_t i = 0; i < n; ++i) out[i] = orc_redc(&c, out[i]);
 }
 
 /* mod_inv_u32 (mul_ntt.cpp:389-403): extended Euclid */
@@ -257,10 +275,19 @@ static uint32_t orc_inv_mod(uint64_t a, uint32_t m) {
     return (uint32_t)t;
 }
 
+/* The CRT inverses, computed once (the reference keeps them in
+ * function-local statics, mul_ntt.cpp:406, 416); set when the library is
+ * loaded, before any thread calls in. */
+static uint64_t orc_inv12, orc_inv123;
+__attribute__((constructor)) static void orc_crt_init(void) {
+    orc_inv12 = orc_inv_mod(ORC_MOD[0], ORC_MOD[1]);
+    orc_inv123 = orc_inv_mod(((uint64_t)ORC_MOD[0] * ORC_MOD[1]) % ORC_MOD[2], ORC_MOD[2]);
+}
+
 /* Garner CRT for two primes (mul_ntt.cpp:405-412) */
 static uint64_t orc_crt2(uint32_t r1, uint32_t r2) {
     const uint64_t m1 = ORC_MOD[0], m2 = ORC_MOD[1];
-    uint64_t inv = orc_inv_mod(m1, (uint32_t)m2);
+    const uint64_t inv = orc_inv12;
     uint64_t d = r2 >= r1 ? (uint64_t)r2 - r1 : (uint64_t)r2 + m2 - r1;
     return r1 + m1 * (d * inv % m2);
 }
@@ -270,7 +297,7 @@ static uint64_t orc_crt2(uint32_t r1, uint32_t r2) {
 static u128 orc_crt3(uint32_t r1, uint32_t r2, uint32_t r3) {
     const uint64_t m1 = ORC_MOD[0], m2 = ORC_MOD[1], m3 = ORC_MOD[2];
     uint64_t x12 = orc_crt2(r1, r2);
-    uint64_t inv = orc_inv_mod((m1 * m2) % m3, (uint32_t)m3);
+    const uint64_t inv = orc_inv123;
     uint64_t x12_m3 = x12 % m3;
     uint64_t d = r3 >= x12_m3 ? r3 - x12_m3 : r3 + m3 - x12_m3;
     return (u128)x12 + (u128)(m1 * m2) * (d * inv % m3);
@@ -282,8 +309,21 @@ static void orc_from_residues(const uint32_t *r1, const uint32_t *r2,
                               const uint32_t *r3, size_t n, uint64_t *out,
                               size_t cap) {
     memset(out, 0, cap * sizeof(uint64_t));
-    u128 carry = 0;
     size_t id = 0;
+    if (!r3) {
+        /* two primes: a coefficient plus the carry stays below 2^64, as in
+         * the reference's 64-bit loop (mul_ntt.cpp:438-445) */
+        uint64_t c64 = 0;
+        for (size_t i = 0; i < n; ++i, ++id) {
+            uint64_t cur = orc_crt2(r1[i], r2[i]) + c64;
+            if ((id >> 2) < cap) out[id >> 2] |= (cur & 0xFFFFu) << ((id & 3) * 16);
+            c64 = cur >> 16;
+        }
+        for (; c64; c64 >>= 16, ++id)
+            if ((id >> 2) < cap) out[id >> 2] |= (c64 & 0xFFFFu) << ((id & 3) * 16);
+        return;
+    }
+    u128 carry = 0;
     for (size_t i = 0; i < n; ++i, ++id) {
         u128 cur = (r3 ? orc_crt3(r1[i], r2[i], r3[i]) : (u128)orc_crt2(r1[i], r2[i])) + carry;
         uint64_t digit = (uint64_t)(cur & 0xFFFFu);

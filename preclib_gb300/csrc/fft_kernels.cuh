@@ -35,7 +35,7 @@ void fft_build_table(double2* tw, cudaStream_t st);
 int fft_configure_kernels();
 // The product's 4 kernels: the first takes the arguments by value and
 // stores them at `d_args` (device) for the others; one graph replay
-// (captured on `cap` once per length and argument buffer), or, with `ev`
+// (built for `cap` once per length and argument buffer), or, with `ev`
 // (or without `cap`), plain launches with an event before the first and
 // after each.  Returns a cudaError_t.  The caller runs one product at a
 // time per argument buffer (its library lane's lock).

@@ -1,289 +1,13 @@
-// ntt_carry.cu -- CRT recombination and carry propagation of the four-step
-// path: the reference's ntt_crt2/ntt_crt3 and serial ntt_from_residues
-// carry loop (src/mul_ntt.cpp:405-487) as one pass over the natural-order
-// residues.
-//
-// Phase 1 (every block): each thread turns 8 coefficients into 4 limbs
-// (set 2: 4 coefficients of up to 150 bits, one per limb, into 4 limbs),
-// the limb carry chain is resolved per warp (ballot) and per block with a
-// block carry-in of 0 (one barrier), the limbs are written, and the block publishes its
-// aggregate (G = carry out, P = a carry-in would pass through).
-// Phase 2 (the last block to finish, found with a fence and an atomic
-// counter): scans the aggregates into per-block carry-ins and adds the
-// carry into the blocks that receive one -- on random data about one block
-// in 64, usually a single limb.  No block ever waits on another.
-#include "ntt_engine.cuh"
+// ntt_carry.cu -- the CRT/carry kernel of the four-step path (one block of
+// crt_carry_tile, ntt_carry.cuh, per CTA), its launchers, and the four-step
+// product's launch sequence.
+#include "ntt_carry.cuh"
 
 namespace precgpu {
 
-constexpr int kBlockLimbs = kCarryThreads * kCarryLimbs;
-
-// ---- set 2: one coefficient per 64-bit limb
-
-// a coefficient c < p1..p5 < 2^150 as three words (w2 < 2^22)
-struct Coef3 {
-    uint64_t w0, w1;
-    uint32_t w2;
-};
-
-// Garner over the five primes (the constants of Crt5Const) from the
-// inverse-transform outputs y_j (any value below 2^32 of each class), then
-// c = v0 + p0 (v1 + p1 (v2 + p2 (v3 + p3 v4))).  LAZY (set 2, p < 2^30):
-// running values in [0, 2p); otherwise (set 3, p < 2^31) in [0, p).
-template <bool LAZY>
-__device__ __forceinline__ Coef3 crt5(const uint32_t (&y)[5], const Crt5Const& cc, const FieldArgs& f) {
-    uint32_t v[5];
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        const uint32_t p = f.pc[j].p, p2 = f.pc[j].p2;
-        if constexpr (LAZY) {
-            uint32_t acc = shoup_lazy(y[j], cc.a[j].w, cc.a[j].wp, p);  // [0, 2p)
-#pragma unroll
-            for (int i = 0; i < j; ++i) {
-                const ShoupC b = cc.b[j * (j - 1) / 2 + i];
-                const uint32_t t = acc + p2 - shoup_lazy(v[i], b.w, b.wp, p);  // (0, 4p)
-                acc = min(t, t - p2);
-            }
-            v[j] = red1(acc, p);
-        } else {
-            uint32_t acc = shoup_mul(y[j], cc.a[j], p);  // [0, p)
-#pragma unroll
-            for (int i = 0; i < j; ++i) acc = sub_mod(acc, shoup_mul(v[i], cc.b[j * (j - 1) / 2 + i], p), p);
-            v[j] = acc;
-        }
-    }
-    u128 X = (u128)((uint64_t)v[4] * f.pc[3].p + v[3]);
-    X = X * f.pc[2].p + v[2];
-    X = X * f.pc[1].p + v[1];  // < 2^120
-    const u128 t0 = (u128)(uint64_t)X * f.pc[0].p + v[0];
-    const u128 t1 = (u128)(uint64_t)(X >> 64) * f.pc[0].p + (uint64_t)(t0 >> 64);
-    Coef3 c;
-    c.w0 = (uint64_t)t0;
-    c.w1 = (uint64_t)t1;
-    c.w2 = (uint32_t)(t1 >> 64);
-    return c;
-}
-
-template <bool LAZY>
-__device__ __forceinline__ Coef3 coef5(const uint32_t* __restrict__ work, uint64_t N, int64_t i,
-                                       const ProdArgs& args) {
-    if (i < 0 || (uint64_t)i >= N) return Coef3{0, 0, 0};
-    uint32_t y[5];
-#pragma unroll
-    for (int j = 0; j < 5; ++j) y[j] = work[(uint64_t)(2 * j) * N + i];
-    return crt5<LAZY>(y, args.crt5, args.f);
-}
-
-// sum of limb m: S_m = w0(c_m) + w1(c_(m-1)) + w2(c_(m-2)) < 2^66
-__device__ __forceinline__ u128 limb_sum(const Coef3& c0, uint64_t w1_prev, uint32_t w2_prev2) {
-    return (u128)c0.w0 + w1_prev + w2_prev2;
-}
-
-struct WideEdge {
-    uint64_t w1;  // w1 of the warp's last coefficient
-    uint32_t w2a, w2b;  // w2 of its last two coefficients
-    uint32_t hi;  // S >> 64 of its last limb
-};
-
-// T[k] = S_(m0+k) for this thread's limbs and hi(S_(m0-1)); the words the
-// first limbs need from below come from the lane below, from the warp
-// below (shared memory), or for the block's first thread from three
-// coefficients computed again by lanes 0..2 of warp 0.
-template <bool LAZY>
-__device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& args, int64_t m0, u128 (&T)[kCarryLimbs],
-                                          uint64_t& prev_hi, WideEdge* s_edge) {
-    static_assert(kCarryLimbs >= 4 && kCarryLimbs % 4 == 0, "limbs per thread: whole 16-byte loads");
-    constexpr int L = kCarryLimbs;
-    const uint64_t N = 1ull << args.k;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    Coef3 c[L];
-    if ((uint64_t)m0 + L <= N) {
-#pragma unroll
-        for (int h = 0; h < L / 4; ++h) {
-            uint4 r[5];
-#pragma unroll
-            for (int j = 0; j < 5; ++j)
-                r[j] = __ldg(reinterpret_cast<const uint4*>(PP.work + (uint64_t)(2 * j) * N + m0) + h);
-            uint32_t y[5];
-#pragma unroll
-            for (int j = 0; j < 5; ++j) y[j] = r[j].x;
-            c[4 * h] = crt5<LAZY>(y, args.crt5, args.f);
-#pragma unroll
-            for (int j = 0; j < 5; ++j) y[j] = r[j].y;
-            c[4 * h + 1] = crt5<LAZY>(y, args.crt5, args.f);
-#pragma unroll
-            for (int j = 0; j < 5; ++j) y[j] = r[j].z;
-            c[4 * h + 2] = crt5<LAZY>(y, args.crt5, args.f);
-#pragma unroll
-            for (int j = 0; j < 5; ++j) y[j] = r[j].w;
-            c[4 * h + 3] = crt5<LAZY>(y, args.crt5, args.f);
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < L; ++k) c[k] = coef5<LAZY>(PP.work, N, m0 + k, args);
-    }
-    const u128 s_last = limb_sum(c[L - 1], c[L - 2].w1, c[L - 3].w2);
-    const uint32_t hi_last = (uint32_t)(s_last >> 64);
-    // words from the thread below: w1(c_-1), w2(c_-1), w2(c_-2), hi(S_-1)
-    uint64_t w1m1 = __shfl_up_sync(0xffffffffu, c[L - 1].w1, 1);
-    uint32_t w2m1 = __shfl_up_sync(0xffffffffu, c[L - 1].w2, 1);
-    uint32_t w2m2 = __shfl_up_sync(0xffffffffu, c[L - 2].w2, 1);
-    uint32_t him1 = __shfl_up_sync(0xffffffffu, hi_last, 1);
-    if (lane == 31) s_edge[warp] = WideEdge{c[L - 1].w1, c[L - 1].w2, c[L - 2].w2, hi_last};
-    if (warp == 0) {
-        // the block's first limb: coefficients m0-1, m0-2, m0-3 (lanes 0, 1, 2)
-        Coef3 e = Coef3{0, 0, 0};
-        const int64_t mb = m0 - lane * L;  // the block's first limb
-        if (lane < 3) e = coef5<LAZY>(PP.work, N, mb - 1 - lane, args);
-        const uint64_t e1w0 = __shfl_sync(0xffffffffu, e.w0, 0);
-        const uint64_t e1w1 = __shfl_sync(0xffffffffu, e.w1, 0);
-        const uint32_t e1w2 = __shfl_sync(0xffffffffu, e.w2, 0);
-        const uint64_t e2w1 = __shfl_sync(0xffffffffu, e.w1, 1);
-        const uint32_t e2w2 = __shfl_sync(0xffffffffu, e.w2, 1);
-        const uint32_t e3w2 = __shfl_sync(0xffffffffu, e.w2, 2);
-        if (lane == 0) {
-            w1m1 = e1w1;
-            w2m1 = e1w2;
-            w2m2 = e2w2;
-            him1 = (uint32_t)(((u128)e1w0 + e2w1 + e3w2) >> 64);
-        }
-    }
-    __syncthreads();
-    if (lane == 0 && warp > 0) {
-        const WideEdge e = s_edge[warp - 1];
-        w1m1 = e.w1;
-        w2m1 = e.w2a;
-        w2m2 = e.w2b;
-        him1 = e.hi;
-    }
-    T[0] = limb_sum(c[0], w1m1, w2m2);
-    T[1] = limb_sum(c[1], c[0].w1, w2m1);
-#pragma unroll
-    for (int k = 2; k < L; ++k) T[k] = limb_sum(c[k], c[k - 1].w1, c[k - 2].w2);
-    prev_hi = him1;
-}
-
-// scratch layout: [0] finished-block counter, [1 .. nblk] aggregates
-// (bit0 G, bit1 P)
 template <int SET>
 __global__ void __launch_bounds__(kCarryThreads) k_crt_carry(ProdArgs args, const ProdPtrs* __restrict__ batch) {
-    __shared__ BlockCarryShared sh;
-    __shared__ uint32_t s_last;
-    __shared__ WideEdge s_edge[kCarryThreads / 32];
-    const ProdPtrs PP = select_product(args, batch);
-    const uint32_t bid = args.crt_blk0 + blockIdx.x;  // chunked CRT: blocks from crt_blk0
-    if ((int)bid >= PP.nblk) return;  // batch: a shorter product of the class
-    const uint64_t N = 1ull << args.k;
-    const int lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)bid * kBlockLimbs + threadIdx.x * kCarryLimbs;
-
-    u128 T[kCarryLimbs];
-    uint64_t prev_hi = 0;
-    if constexpr (set_wide(SET)) {
-        wide_sums<SET == kWideSet>(PP, args, m0, T, prev_hi, s_edge);
-    } else {
-        const uint32_t* __restrict__ r0 = PP.work;
-        const uint32_t* __restrict__ r1 = PP.work + 2 * N;
-        const uint32_t* __restrict__ r2 = PP.work + 4 * N;
-        const uint64_t i0 = 2 * (uint64_t)m0;
-        if (i0 + 2 * kCarryLimbs <= N) {
-            uint32_t y[3][2 * kCarryLimbs];
-#pragma unroll
-            for (int h = 0; h < 2 * kCarryLimbs / 4; ++h) {
-                const uint4 a = __ldg(reinterpret_cast<const uint4*>(r0 + i0) + h);
-                const uint4 b = __ldg(reinterpret_cast<const uint4*>(r1 + i0) + h);
-                const uint4 c = __ldg(reinterpret_cast<const uint4*>(r2 + i0) + h);
-                y[0][4 * h] = a.x; y[0][4 * h + 1] = a.y; y[0][4 * h + 2] = a.z; y[0][4 * h + 3] = a.w;
-                y[1][4 * h] = b.x; y[1][4 * h + 1] = b.y; y[1][4 * h + 2] = b.z; y[1][4 * h + 3] = b.w;
-                y[2][4 * h] = c.x; y[2][4 * h + 1] = c.y; y[2][4 * h + 2] = c.z; y[2][4 * h + 3] = c.w;
-            }
-#pragma unroll
-            for (int k = 0; k < kCarryLimbs; ++k) {
-                const u128 c0 = crt3(y[0][2 * k], y[1][2 * k], y[2][2 * k], args.crt, args.f);
-                const u128 c1 = crt3(y[0][2 * k + 1], y[1][2 * k + 1], y[2][2 * k + 1], args.crt, args.f);
-                T[k] = c0 + (c1 << 32);
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < kCarryLimbs; ++k) {
-                u128 c[2];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const uint64_t i = i0 + 2 * k + e;
-                    c[e] = i < N ? crt3(r0[i], r1[i], r2[i], args.crt, args.f) : (u128)0;
-                }
-                T[k] = c[0] + (c[1] << 32);
-            }
-        }
-        // hi(T) of the limb just below this thread's first limb
-        prev_hi = __shfl_up_sync(0xffffffffu, (uint64_t)(T[kCarryLimbs - 1] >> 64), 1);
-        if (lane == 0) {
-            prev_hi = 0;
-            if (m0 > 0 && i0 - 1 < N) {
-                const u128 c0 = crt3(r0[i0 - 2], r1[i0 - 2], r2[i0 - 2], args.crt, args.f);
-                const u128 c1 = crt3(r0[i0 - 1], r1[i0 - 1], r2[i0 - 1], args.crt, args.f);
-                prev_hi = (uint64_t)((c0 + (c1 << 32)) >> 64);
-            }
-        }
-    }
-    uint64_t v[kCarryLimbs];
-    uint32_t gbits;
-    bool G, P;
-    limbs_from_sums<kCarryLimbs>(T, prev_hi, v, gbits, G, P);
-
-    uint32_t* agg = PP.scratch + 1;
-    auto publish = [&](bool Gb, bool Pb) { agg[bid] = (Gb ? 1u : 0u) | (Pb ? 2u : 0u); };
-    const bool cin = block_carry_in0(G, P, sh, publish);
-    limbs_finish<kCarryLimbs>(m0, PP.lout, v, gbits, cin, PP.out);
-
-    // ---- phase 2: the last block resolves the carries between blocks.
-    // The barrier orders every thread's limb and aggregate stores before
-    // thread 0's device-scope fence, which orders them before the counter.
-    // A chunked CRT (one launch per run of blocks, in order on one stream)
-    // joins each chunk on its own: the carry into the chunk comes from the
-    // previous chunk's join, and its carry out goes to the next.
-    const bool chunked = args.chunk_words != nullptr;
-    uint32_t* counter = chunked ? &args.chunk_words[2 * args.crt_chunk] : &PP.scratch[0];
-    const int blo = chunked ? args.crt_blk0 : 0;
-    const int bhi = chunked ? args.crt_blk0 + (int)gridDim.x : PP.nblk;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = atomicAdd(counter, 1u) == (uint32_t)(bhi - blo) - 1 ? 1u : 0u;
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    const bool cin_chunk = chunked && __ldcg(&args.chunk_words[2 * args.crt_chunk + 1]) != 0;
-    const int nb = bhi - blo;
-    const int per = (nb + blockDim.x - 1) / blockDim.x;  // aggregates per thread
-    const int b0 = blo + threadIdx.x * per, b1 = min(b0 + per, bhi);
-    // this thread's run of blocks as one carry element
-    bool tG = false, tP = true;
-    for (int b = b0; b < b1; ++b) {
-        const uint32_t a = __ldcg(&agg[b]);
-        tG = (a & 1u) || (tG && (a & 2u));
-        tP = tP && (a & 2u);
-    }
-    auto chunk_in = [&](bool, bool) -> bool { return cin_chunk; };
-    bool c = block_carry(tG, tP, sh, chunk_in);  // carry into this thread's first block
-    for (int b = b0; b < b1; ++b) {
-        const uint32_t a = __ldcg(&agg[b]);
-        if (c) {
-            // the carry enters block b: +1 ripples through its all-ones limbs
-            const uint64_t lim_end = min((uint64_t)(b + 1) * kBlockLimbs, PP.lout);
-            for (uint64_t m = (uint64_t)b * kBlockLimbs; m < lim_end; ++m) {
-                const uint64_t x = __ldcg(&PP.out[m]) + 1;
-                PP.out[m] = x;
-                if (x != 0) break;
-            }
-        }
-        c = (a & 1u) || (c && (a & 2u));
-    }
-    if (b0 < bhi && b1 == bhi) {  // the thread holding the last block
-        if (chunked && !args.crt_last) args.chunk_words[2 * args.crt_chunk + 3] = c ? 1u : 0u;
-        else if (c) atomicOr(args.err, kDevErrCarry);  // a product fits La+Lb limbs
-    }
+    crt_carry_tile<SET>(args, batch, GridIdx{});
 }
 
 void launch_crt_carry(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs* batch, int count, int max_nblk,
@@ -363,6 +87,7 @@ int ntt_configure_kernels() {
     if (!e) e = configure_inv_cols();
     if (!e) e = configure_rows();
     if (!e) e = configure_small();
+    if (!e) e = configure_class();
     return e;
 }
 

@@ -7,8 +7,10 @@
 //   first log2(N1) stages of ntt_forward, mul_ntt.cpp:193-255) and
 //   multiplied by the four-step twiddle w_N^(i2*k1).  Output row slot s
 //   holds frequency k1 = bitrev(s).
-// k_inv_cols: the inverse four-step twiddle w_N^-(i2*k1), then the DIT
-//   transform over the row slots (the last stages of ntt_inverse,
+// k_inv_cols: the inverse four-step twiddle w_N^-(i2*k1) times the prime's
+//   CRT scale (CrtConst/Crt5Const::fold: the Garner constant that would
+//   otherwise cost the CRT one product per prime and coefficient), then the
+//   DIT transform over the row slots (the last stages of ntt_inverse,
 //   mul_ntt.cpp:257-329) back to natural coefficient order.
 // Both generate their twiddles as running Montgomery powers over a thread's
 // 32 slots of one column (twiddle32).
@@ -58,138 +60,63 @@ __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __
     }
 }
 
+// The forward column pass: column group x (C columns) and y = prime*2 +
+// operand (or just the prime for a square or a launch of one operand) of
+// product z; nx = column groups per (prime, operand).
 template <int SET, int M, int C, int MR>
 __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
-    constexpr int NP = sch_np(M, MR);
-    static_assert(NP >= 2, "column transforms have at least two passes");
-    const ProdPtrs P = select_product(args, batch);
-    // grid.y: prime*2 + operand, or just the prime for a square or a
-    // launch of one operand
-    const bool one = args.square || args.operand_only;
-    const int prime = args.prime0 + (one ? blockIdx.y : blockIdx.y >> 1);
-    const int operand = args.operand_only ? args.operand_only - 1 : (one ? 0 : blockIdx.y & 1);
-    const PrimeC pc = args.f.pc[prime];
-    const uint2* __restrict__ tw = args.f.tf[prime];
-    const uint32_t N2 = 1u << args.k2;
-    const uint32_t c0 = blockIdx.x * C;
-    // a graph replay's later kernels read the product from `publish`
-    if (args.publish && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *args.publish = P;
-
-    // the carry kernel's look-back words start at zero
-    if (blockIdx.y == 0 && args.prime0 == 0) {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= P.nblk; i += gridDim.x * blockDim.x)
-            P.scratch[i] = 0;
-    }
-
-    if constexpr (set_wide(SET)) {
-        // one digit per limb; the plan puts both operands in the lower half
-        const uint64_t nl = operand ? P.lb : P.la;
-        if (nl > (1ull << (args.k - 1))) {
-            if (threadIdx.x == 0) atomicOr(args.err, kDevErrPlan);
-            return;
-        }
-        stage_limbs<M, C>(sm, operand ? P.b : P.a, N2, c0, nl);
-        __syncthreads();
-        col_top_upper_zero<SET, M, C, MR>(sm, tw, pc);
-    } else {
-        const uint32_t* __restrict__ dig = reinterpret_cast<const uint32_t*>(operand ? P.b : P.a);
-        const uint64_t nd = 2 * (operand ? P.lb : P.la);
-        // the column tile of raw digits, staged by 16-byte asynchronous copies
-        // (digits past the operand read as zero), then the top pass reduces them
-        if (nd <= (1ull << (args.k - 1))) {
-            stage_rows<M, C>(sm, dig, N2, c0, nd, 0, 1 << (M - 1));
-            cp_async_wait<0>();
-            __syncthreads();
-            col_top_upper_zero<SET, M, C, MR>(sm, tw, pc);
-        } else {
-            stage_cols<M, C>(sm, dig, N2, c0, nd);
-            __syncthreads();
-            col_pass<SET, M, 0, false, C, true, MR>(sm, tw, pc);
-        }
-    }
-    __syncthreads();
-    col_passes<SET, M, 1, NP - 2, false, C, MR>(sm, tw, pc);
-    {   // bottom pass (bits 0..4) with the four-step twiddle, straight to HBM
-        using G = Geom<M, NP - 1, MR>;
-        static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
-        uint32_t* __restrict__ dst = P.work + ((uint64_t)(prime * 2 + operand) << args.k);
-        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
-            const int col = w & (C - 1);
-            const uint32_t u = w / C;
-            const uint32_t* s = sm + (33 * u) * C + col;
-            uint32_t x[1][32];
-#pragma unroll
-            for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
-            regs_pass<SET, M, NP - 1, false, 1, MR>(x, u, tw, pc);
-            // slot 32u + q holds k1 = brev5(q) << (M-5) | brev(u): the twiddle
-            // w^(i2*k1) is t * g^brev5(q) with t = w^(i2*brev(u)), g = w^(i2 << (M-5))
-            const uint32_t i2 = c0 + col;
-            const uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), args.k);
-            const uint32_t g = fourstep_twiddle<SET>(args.f, prime, i2 << (M - 5), args.k);
-            twiddle32<SET>(x[0], t, g, pc);
-#pragma unroll
-            for (int q = 0; q < 32; ++q) dst[(uint64_t)(32 * u + q) * N2 + i2] = x[0][q];
-        }
-    }
+#define PREC_TILE_X blockIdx.x
+#define PREC_TILE_Y blockIdx.y
+#define PREC_TILE_NX gridDim.x
+#define PREC_TILE_PRODUCT select_product(args, batch)
+#include "ntt_cols_fwd_body.inc"
+#undef PREC_TILE_X
+#undef PREC_TILE_Y
+#undef PREC_TILE_NX
+#undef PREC_TILE_PRODUCT
 }
 
+// One tile of the forward column pass at the indices ix (a persistent kernel's).
+template <int SET, int M, int C, int MR>
+__device__ __forceinline__ void fwd_cols_tile(const ProdArgs& args, const ProdPtrs* __restrict__ batch,
+                                              const TileIdx& ix, uint32_t* sm) {
+#define PREC_TILE_X ix.bx
+#define PREC_TILE_Y ix.by
+#define PREC_TILE_NX ix.nbx
+#define PREC_TILE_PRODUCT select_product_at(args, batch, ix.bz)
+#include "ntt_cols_fwd_body.inc"
+#undef PREC_TILE_X
+#undef PREC_TILE_Y
+#undef PREC_TILE_NX
+#undef PREC_TILE_PRODUCT
+}
+
+// The inverse column pass: column group x, prime args.prime0 + y of
+// product z.
 template <int SET, int M, int C, int MR>
 __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_inv_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
-    constexpr int NP = sch_np(M, MR);
-    static_assert(NP >= 2, "column transforms have at least two passes");
-    const ProdPtrs P = select_product(args, batch);
-    const int prime = args.prime0 + blockIdx.y;
-    const PrimeC pc = args.f.pc[prime];
-    const uint2* __restrict__ tw = args.f.ti[prime];
-    const uint32_t N2 = 1u << args.k2;
-    const uint32_t c0 = blockIdx.x * C;
-    uint32_t* __restrict__ wk = P.work + ((uint64_t)(prime * 2) << args.k);
-    // the column tile, staged by 16-byte asynchronous copies
-    stage_cols<M, C>(sm, wk, N2, c0, ~0ull);
-    __syncthreads();
-    {   // bottom DIT pass (bits 0..4) after the inverse four-step twiddle
-        using G = Geom<M, NP - 1, MR>;
-        static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
-        const uint32_t nmask = (uint32_t)((1ull << args.k) - 1);
-        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
-            const int col = w & (C - 1);
-            const uint32_t u = w / C;
-            uint32_t* s = sm + (33 * u) * C + col;
-            uint32_t x[1][32];
-#pragma unroll
-            for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
-            // slot 32u + q holds k1 = brev5(q) << (M-5) | brev(u): the twiddle
-            // w^-(i2*k1) is t * g^brev5(q), t = w^-(i2*brev(u)), g = w^-(i2 << (M-5));
-            // the row pass left every value in the forward range
-            const uint32_t i2 = c0 + col;
-            const uint32_t t = fourstep_twiddle<SET>(args.f, prime, (0u - i2 * brev_bits(u, M - 5)) & nmask, args.k);
-            const uint32_t g = fourstep_twiddle<SET>(args.f, prime, (0u - (i2 << (M - 5))) & nmask, args.k);
-            twiddle32<SET>(x[0], t, g, pc);
-            regs_pass<SET, M, NP - 1, true, 1, MR>(x, u, tw, pc);
-#pragma unroll
-            for (int q = 0; q < 32; ++q) s[q * C] = x[0][q];
-        }
-        __syncthreads();
-    }
-    col_passes<SET, M, NP - 2, 1, true, C, MR>(sm, tw, pc);
-    {   // top DIT pass: natural row order i1, straight to HBM
-        using G = Geom<M, 0, MR>;
-        for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
-            const int col = w & (C - 1);
-            const uint32_t u = w / C;
-            const uint32_t* s = sm + G::pbase(u) * C + col;
-            uint32_t x[1][G::R];
-#pragma unroll
-            for (int q = 0; q < G::R; ++q) x[0][q] = s[q * G::QS * C];
-            regs_pass<SET, M, 0, true, 1, MR>(x, u, tw, pc);
-            const uint32_t base = G::base(u);
-#pragma unroll
-            for (int q = 0; q < G::R; ++q)
-                wk[(uint64_t)(base + ((uint32_t)q << G::LO)) * N2 + c0 + col] = x[0][q];
-        }
-    }
+#define PREC_TILE_X blockIdx.x
+#define PREC_TILE_Y blockIdx.y
+#define PREC_TILE_PRODUCT select_product(args, batch)
+#include "ntt_cols_inv_body.inc"
+#undef PREC_TILE_X
+#undef PREC_TILE_Y
+#undef PREC_TILE_PRODUCT
+}
+
+// One tile of the inverse column pass at the indices ix.
+template <int SET, int M, int C, int MR>
+__device__ __forceinline__ void inv_cols_tile(const ProdArgs& args, const ProdPtrs* __restrict__ batch,
+                                              const TileIdx& ix, uint32_t* sm) {
+#define PREC_TILE_X ix.bx
+#define PREC_TILE_Y ix.by
+#define PREC_TILE_PRODUCT select_product_at(args, batch, ix.bz)
+#include "ntt_cols_inv_body.inc"
+#undef PREC_TILE_X
+#undef PREC_TILE_Y
+#undef PREC_TILE_PRODUCT
 }
 
 // ---------------------------------------------------------------------------

@@ -376,6 +376,26 @@ __device__ __forceinline__ u128 crt3(uint32_t y1, uint32_t y2, uint32_t y3, cons
     return (u128)t * p1 + v1;
 }
 
+// crt3 of the four-step path: the inverse column pass has already
+// multiplied y_j by s1, k22, k33 (CrtConst::fold), so y_j is v1's, and
+// v2's and v3's first term.  Set 0 leaves y_j in [0, 4p), set 1 in [0, p).
+template <int SET>
+__device__ __forceinline__ u128 crt3_folded(uint32_t y1, uint32_t y2, uint32_t y3, const CrtConst& cc,
+                                            const FieldArgs& f) {
+    const uint32_t p1 = f.pc[0].p, p2 = f.pc[1].p, p3 = f.pc[2].p;
+    if constexpr (SET == 0) {
+        y1 = red1(red1(y1, f.pc[0].p2), p1);
+        y2 = red1(red1(y2, f.pc[1].p2), p2);
+        y3 = red1(red1(y3, f.pc[2].p2), p3);
+    }
+    const uint32_t v1 = y1;
+    const uint32_t v2 = sub_mod(y2, shoup_mul(v1, cc.k21, p2), p2);
+    uint32_t v3 = sub_mod(y3, shoup_mul(v1, cc.k31, p3), p3);
+    v3 = sub_mod(v3, shoup_mul(v2, cc.k32, p3), p3);
+    const uint64_t t = (uint64_t)v2 + (uint64_t)p2 * v3;
+    return (u128)t * p1 + v1;
+}
+
 // Carry-in of every lane from the lanes' (G, P) bits: the chain
 // c_{t+1} = G_t | (P_t & c_t) is the carry chain of the sum A + B with
 // A = G|P, B = G (G and P are disjoint), so the carry into lane t is bit t

@@ -25,18 +25,27 @@ struct FieldArgs {
 };
 
 // CRT constants of one transform length (Garner with the transform's
-// scale 2^32 * N^-1 folded in; see crt3 in ntt_engine.cuh).
+// scale 2^32 * N^-1 folded in; see crt3 in ntt_engine.cuh).  The
+// single-CTA path multiplies prime j's outputs by sigma_j in the CRT (s1,
+// k22, k33 hold sigma_1, sigma_2 c12, sigma_3 c13 c23); the four-step path
+// applies those products in its inverse column pass instead, through
+// fold[j] = (that constant) * 2^32 mod p_j (Montgomery form) on the running
+// twiddle, and its CRT multiplies by k21, k31, k32 only.
 struct CrtConst {
     ShoupC s1, k21, k22, k31, k32, k33;
+    uint32_t fold[3];
 };
 
 // Garner constants of the five-prime set for one transform length:
 // v_j = y_j * a_j - sum_{i<j} v_i * b_{ij} (mod p_j), with
-// a_j = 2^32 N^-1 (p_1 .. p_{j-1})^-1 and b_{ij} = (p_i .. p_{j-1})^-1 mod p_j;
-// b_{ij} is b[j(j-1)/2 + i] (primes counted from 0).
+// a_j = 2^32 N^-1 (p_0 .. p_{j-1})^-1 and b_{ij} = (p_i .. p_{j-1})^-1 mod p_j;
+// b_{ij} is b[j(j-1)/2 + i] (primes counted from 0).  The inverse column
+// pass multiplies prime j's values by a_j (fold[j] = a_j * 2^32 mod p_j,
+// Montgomery form, on its running twiddle), so the CRT starts from
+// y_j * a_j directly.
 struct Crt5Const {
-    ShoupC a[5];
     ShoupC b[10];
+    uint32_t fold[5];
 };
 
 struct ProdPtrs;
@@ -87,8 +96,9 @@ struct ProdPtrs {
 // the product this CTA works on: the launch's own arguments, or entry
 // blockIdx.z of a batch's descriptor array (a separate value, so the kernel
 // parameter block is never written and stays in the constant bank)
-__device__ __forceinline__ ProdPtrs select_product(const ProdArgs& args, const ProdPtrs* __restrict__ batch) {
-    if (batch) return batch[blockIdx.z];
+__device__ __forceinline__ ProdPtrs select_product_at(const ProdArgs& args, const ProdPtrs* __restrict__ batch,
+                                                      uint32_t z) {
+    if (batch) return batch[z];
     ProdPtrs p;
     p.a = args.a;
     p.b = args.b;
@@ -101,6 +111,26 @@ __device__ __forceinline__ ProdPtrs select_product(const ProdArgs& args, const P
     p.nblk = args.nblk;
     p.pad = 0;
     return p;
+}
+// Where a tile of a four-step pass finds its indices: GridIdx (one tile per
+// CTA) reads blockIdx/gridDim where they are used, exactly as a kernel
+// written for one tile does; TileIdx carries the indices a persistent kernel
+// assigned.
+struct GridIdx {
+    __device__ __forceinline__ uint32_t x() const { return blockIdx.x; }
+    __device__ __forceinline__ uint32_t y() const { return blockIdx.y; }
+    __device__ __forceinline__ uint32_t z() const { return blockIdx.z; }
+    __device__ __forceinline__ uint32_t nx() const { return gridDim.x; }
+};
+struct TileIdx {
+    uint32_t bx, by, bz, nbx;
+    __device__ __forceinline__ uint32_t x() const { return bx; }
+    __device__ __forceinline__ uint32_t y() const { return by; }
+    __device__ __forceinline__ uint32_t z() const { return bz; }
+    __device__ __forceinline__ uint32_t nx() const { return nbx; }
+};
+__device__ __forceinline__ ProdPtrs select_product(const ProdArgs& args, const ProdPtrs* __restrict__ batch) {
+    return select_product_at(args, batch, blockIdx.z);
 }
 #endif
 
@@ -264,6 +294,28 @@ inline void col_config(int set, int m, int req_cg, int req_mr, int& cg, int& mr)
 }
 int configure_rows();
 int configure_small();
+int configure_class();
+
+// The batch form's persistent kernel per length class (ntt_class.cu): its
+// scheduling words, zeroed before each launch, are kClassHdrWords (the next
+// work item, the abort word) then kClassProdWords per product (forward
+// column tiles done per prime, row tiles done per prime, inverse column
+// tiles done).
+constexpr int kClassHdrWords = 2;
+constexpr int kClassProdWords = 7;
+struct ClassRun {
+    uint32_t* sched;      // the scheduling words
+    int count;            // products of this launch (entries of the descriptor array)
+    int max_nblk;         // carry blocks of its longest product
+    int rows;             // row slots per row tile (class_rows)
+    uint32_t spin_limit;  // polls before a dependency wait gives up (about 0.25 us each)
+    int never_signal;     // tests: forward tiles leave their counters untouched
+};
+// row slots per row tile of the class kernel (256 threads)
+int class_rows(int k1, int k2);
+// one launch of the class kernel for `run.count` products of batch; -1 when
+// the configuration is not instantiated
+int launch_class_persistent(const ProdArgs& a, const ProdPtrs* batch, const ClassRun& run, cudaStream_t st);
 
 // out[0 .. n) += t[0 .. nt) (nt <= n), the carry running on into out's
 // higher limbs (ntt_add.cu); scratch holds add_into_scratch_words(nt)

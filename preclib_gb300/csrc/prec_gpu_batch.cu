@@ -11,9 +11,12 @@
 //     all their products (grid.z = product, per-product pointers in a
 //     device descriptor array), in chunks bounded by a workspace budget;
 //   * each class gets its own stream branch, so classes overlap on the GPU;
-//   * the first prec_gpu_batch_run captures all of it into one CUDA graph
+//   * the first prec_gpu_batch_run records all of it into one CUDA graph
 //     (descriptors and workspaces have fixed addresses), later runs replay
-//     the graph with a single launch.
+//     the graph with a single launch;
+//   * with PREC_GPU_BATCH_PERSISTENT=1, set 0's 2^13 .. 2^16-point classes
+//     run as one persistent kernel per class (ntt_class.cu) instead of four
+//     phase kernels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,6 +49,8 @@ struct Cls {
     SmallDesc* d_small = nullptr; // device descriptors (single-CTA classes)
     ProdPtrs* d_ptrs = nullptr;   // device descriptors (four-step classes)
     uint8_t* ws = nullptr;        // workspace of one chunk
+    bool persistent = false;      // one persistent kernel per chunk (ntt_class.cu)
+    uint32_t* sched = nullptr;    // its scheduling words (kClassHdrWords + kClassProdWords per product)
     cudaStream_t stream = nullptr;
     cudaEvent_t join = nullptr;
 };
@@ -73,8 +78,10 @@ struct prec_gpu_batch {
     cudaEvent_t fork = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    uint64_t graph_launches = 0;  // kernels in the captured graph
+    uint64_t graph_launches = 0;  // kernels in the recorded graph
     int* err = nullptr;
+    uint32_t spin_limit = 0;      // persistent class kernels: polls per dependency wait
+    int never_signal = 0;         // tests: their forward tiles never complete a counter
 };
 
 static void batch_free(prec_gpu_batch* b) {
@@ -135,8 +142,17 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
             args.crt = c.pl.crt;
             args.crt5 = c.pl.crt5;
             args.f = ctx_field(c.pl.set);
-            for (const Chunk& ch : c.chunks)
+            for (const Chunk& ch : c.chunks) {
+                if (c.persistent) {
+                    const size_t bytes = (kClassHdrWords + (size_t)kClassProdWords * ch.count) * sizeof(uint32_t);
+                    if (rec) rec->add_memset(c.sched, bytes, st);
+                    else cudaMemsetAsync(c.sched, 0, bytes, st);
+                    const ClassRun run{c.sched, ch.count, ch.max_nblk, class_rows(c.pl.k1, c.pl.k2), b->spin_limit,
+                                       b->never_signal};
+                    if (launch_class_persistent(args, c.d_ptrs + ch.first, run, st) == 0) continue;
+                }
                 ntt_launch_4step_batch(c.pl.set, args, c.d_ptrs + ch.first, ch.count, ch.max_nblk, st);
+            }
         }
         if (branch && !rec) {
             cudaEventRecord(c.join, st);
@@ -201,7 +217,17 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
         c.items.push_back((int)i);
     }
     // device layout: descriptors, then one workspace per four-step class
+    // (and, for a persistent class, its scheduling words)
     const size_t budget = env_bytes("PREC_GPU_BATCH_CLASS_BYTES", (size_t)1 << 30);
+    const char* pe = std::getenv("PREC_GPU_BATCH_PERSISTENT");
+    const bool persistent = pe && pe[0] == '1';
+    // a dependency wait gives up after about a second (PREC_GPU_BATCH_SPIN_LIMIT polls
+    // of ~0.25 us; tests shorten it); PREC_GPU_BATCH_NEVER_SIGNAL=1 (tests)
+    // makes every such wait run out
+    b->spin_limit = (uint32_t)env_bytes("PREC_GPU_BATCH_SPIN_LIMIT", (size_t)1 << 22);
+    const char* ns = std::getenv("PREC_GPU_BATCH_NEVER_SIGNAL");
+    b->never_signal = ns && ns[0] == '1' ? 1 : 0;
+    std::vector<size_t> sched_off;
     size_t bytes = 0;
     std::vector<size_t> desc_off, ws_off;
     for (auto& kv : by_k) {
@@ -218,8 +244,12 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             c.per_chunk = (int)std::min<size_t>({n, std::max<size_t>(1, budget / c.ws_per), 65535});
             ws_off.push_back(bytes);
             bytes += c.ws_per * c.per_chunk;
+            c.persistent = persistent && class_persistent_supported(c.pl);
+            sched_off.push_back(bytes);
+            if (c.persistent) bytes += align256((kClassHdrWords + (size_t)kClassProdWords * c.per_chunk) * sizeof(uint32_t));
         } else {
             ws_off.push_back(0);
+            sched_off.push_back(0);
         }
         b->classes.push_back(c);
     }
@@ -257,6 +287,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             BCK(upload(c.d_small, h.data(), n * sizeof(SmallDesc)));
         } else {
             c.ws = base + ws_off[ci];
+            if (c.persistent) c.sched = reinterpret_cast<uint32_t*>(base + sched_off[ci]);
             std::vector<ProdPtrs> h(n);
             const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
             for (size_t j = 0; j < n; ++j) {

@@ -8,7 +8,7 @@
 //     prime and direction serves every transform length);
 //   * per calling thread, a lane (Lane): a stream for the host-pointer
 //     entry points, a workspace and staging buffers that grow to the
-//     largest product the thread has made, and its captured graphs, so
+//     largest product the thread has made, and its graphs, so
 //     products from different threads overlap on the device.
 #include <cuda_runtime.h>
 
@@ -139,6 +139,9 @@ static CrtConst crt_compute(int set, int k) {
     c.k31 = shoup(c1323, p3);
     c.k32 = shoup(c23, p3);
     c.k33 = shoup(mulmod(s[2], c1323, p3), p3);
+    c.fold[0] = mulmod(c.s1.w, (uint32_t)((1ull << 32) % p1), p1);
+    c.fold[1] = mulmod(c.k22.w, (uint32_t)((1ull << 32) % p2), p2);
+    c.fold[2] = mulmod(c.k33.w, (uint32_t)((1ull << 32) % p3), p3);
     return c;
 }
 
@@ -153,7 +156,7 @@ static Crt5Const crt5_compute(int set, int k) {
         const uint32_t R = (uint32_t)((1ull << 32) % p);
         uint32_t a = mulmod(R, invmod((uint32_t)((1ull << k) % p), p), p);
         for (int i = 0; i < j; ++i) a = mulmod(a, invmod(P[i] % p, p), p);
-        c.a[j] = shoup(a, p);
+        c.fold[j] = mulmod(a, R, p);
         for (int i = 0; i < j; ++i) {
             uint32_t b = 1;
             for (int l = i; l < j; ++l) b = mulmod(b, invmod(P[l] % p, p), p);
@@ -243,7 +246,7 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
 
 // A single four-step product up to 2^kGraphMaxLog2 points runs as one CUDA
 // graph replay: its kernels are the batch form's with a one-entry
-// descriptor array, captured once per plan shape; each call uploads the
+// descriptor array, built once per plan shape; each call uploads the
 // descriptor (operands, output, workspace, sizes) and launches the graph.
 // Below 2^19 points the four kernels take only a few microseconds each,
 // so launching them one by one left the GPU waiting on the host.
@@ -269,7 +272,7 @@ struct GraphEntry {
 
 // One calling thread's resources (a "lane"): its streams, the per-product
 // workspace and staging buffers, the status block a host product reads
-// back, events, per-prime streams and captured single-product graphs.
+// back, events, per-prime streams and single-product graphs.
 // Products on different lanes run concurrently on the GPU; a lane runs one
 // product at a time (mu).  A thread takes a lane on its first call and
 // keeps it; past kMaxLanes threads, threads share lanes round-robin.  (The
@@ -279,7 +282,7 @@ constexpr int kMaxLanes = 16;
 struct Lane {
     std::mutex mu;
     cudaStream_t stream = nullptr;  // host-pointer products
-    cudaStream_t cap = nullptr;     // capture stream of this lane's graphs
+    cudaStream_t cap = nullptr;     // the stream handle this lane's graph nodes are recorded for
     // host products with a chunked CRT: each chunk's limbs copy out on
     // `copy` while the next chunks run
     cudaStream_t copy = nullptr;
@@ -694,7 +697,7 @@ static int ensure_io(Lane& L, size_t limbs) {
 // Enqueues one NTT-band product on device pointers.
 // A square (d_a == d_b, la == lb) transforms its one operand only on the
 // four-step path; the single-CTA path reads the operand twice.
-// One four-step product as a replay of its shape's graph (captured on first
+// One four-step product as a replay of its shape's graph (built on first
 // use).  The forward column kernel takes the product by value -- a replay
 // sets that node's parameters -- and stores its descriptor for the row,
 // inverse column and carry kernels, which run in batch form on it.  (An

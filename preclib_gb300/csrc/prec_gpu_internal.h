@@ -68,6 +68,11 @@ int wide_set(int kw);
 // 64-bit digits allowed (prec_gpu_set_wide_digits; PREC_GPU_WIDE_DIGITS)
 bool wide_digits();
 
+// Whether a batch class of plan `pl` can run as one persistent kernel
+// (ntt_class.cu: set 0's 2^13 .. 2^16-point classes in their default
+// kernel configuration).
+bool class_persistent_supported(const Plan& pl);
+
 // Kernel configuration of one four-step transform length (the autotuner's
 // unit; prec_gpu_tune.cu).
 struct KernelConfig {

@@ -134,6 +134,9 @@ static CrtConst na_crt(int k) {
     c.k31 = na_shoup(c1323, p3);
     c.k32 = na_shoup(c23, p3);
     c.k33 = na_shoup(na_mulmod(s[2], c1323, p3), p3);
+    c.fold[0] = na_mulmod(c.s1.w, (uint32_t)((1ull << 32) % p1), p1);
+    c.fold[1] = na_mulmod(c.k22.w, (uint32_t)((1ull << 32) % p2), p2);
+    c.fold[2] = na_mulmod(c.k33.w, (uint32_t)((1ull << 32) % p3), p3);
     return c;
 }
 

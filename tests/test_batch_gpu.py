@@ -157,3 +157,85 @@ def test_batch_both_digit_widths(gpu):
         a, b = db.operands(i)
         if len(a) and len(b):
             assert np.array_equal(db.result(i), O.mul_ntt(a, b)), sizes[i]
+
+
+def _mid_class_sizes(seed, count):
+    """Products whose transforms have 2^13 .. 2^16 points on 32-bit digits
+    (the persistent class kernel's classes), squares among them."""
+    rng = np.random.default_rng(seed)
+    sizes = []
+    for i in range(count):
+        k = 13 + i % 4
+        # an + bn in (2^(k-2), 2^(k-1)]: 2*(an+bn) - 1 digits need 2^k points
+        total = int(rng.integers((1 << (k - 2)) + 2, (1 << (k - 1)) + 1))
+        if i % 5 == 4:
+            sizes.append((total // 2, total // 2))
+        else:
+            an = int(rng.integers(1, total))
+            sizes.append((an, total - an))
+    return sizes
+
+
+def test_batch_persistent_class_kernel(gpu, monkeypatch):
+    """PREC_GPU_BATCH_PERSISTENT=1: the 2^13 .. 2^16-point classes run as one
+    persistent kernel each (work items from a ticket, bounded waits on
+    per-product phase counters).  Every product equals the oracle, on the
+    first run and on a graph replay with new operand values."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("PREC_GPU_BATCH_PERSISTENT", "1")
+    sizes = _mid_class_sizes(21, 160)
+    db = DevBatch(torch, sizes, 900)
+    sq = [i for i, (a, b) in enumerate(sizes) if a == b]
+    items = db.items()
+    for i in sq:  # a square: the same operand pointer twice
+        items[i] = (items[i][0], sizes[i][0], items[i][0], sizes[i][0], items[i][4])
+    batch = gpu.Batch(items)
+    stream = torch.cuda.current_stream().cuda_stream
+    c0 = gpu.launch_count()
+    for rnd in range(2):
+        if rnd:
+            db.fill(7000)
+        db.out.fill_(-1)
+        batch.run(stream)
+        gpu.stream_check(stream)
+        for i, (an, bn) in enumerate(sizes):
+            a, b = db.operands(i)
+            if i in sq:
+                b = a
+            assert np.array_equal(db.result(i), O.mul_ntt(a, b)), (rnd, i, sizes[i])
+    # one kernel per class per run: 4 lengths, products and squares apart
+    # (8 classes), not 4 phase kernels each
+    assert gpu.launch_count() - c0 == 2 * 8
+    batch.close()
+
+
+def test_batch_persistent_wait_runs_out(gpu, monkeypatch):
+    """A dependency wait of the persistent class kernel that can never be
+    satisfied (PREC_GPU_BATCH_NEVER_SIGNAL=1: the forward tiles leave their
+    counters untouched) gives up after its poll limit: the run ends, the
+    stream check reports PREC_GPU_E_TIMEOUT, and the context stays usable
+    (a normal batch afterwards is exact)."""
+    torch = pytest.importorskip("torch")
+    from preclib_gb300.native import E_TIMEOUT, PrecGpuError
+    sizes = _mid_class_sizes(22, 12)
+    db = DevBatch(torch, sizes, 300)
+    stream = torch.cuda.current_stream().cuda_stream
+    monkeypatch.setenv("PREC_GPU_BATCH_PERSISTENT", "1")
+    monkeypatch.setenv("PREC_GPU_BATCH_NEVER_SIGNAL", "1")
+    monkeypatch.setenv("PREC_GPU_BATCH_SPIN_LIMIT", "4000")
+    batch = gpu.Batch(db.items())
+    batch.run(stream)
+    with pytest.raises(PrecGpuError) as ei:
+        gpu.stream_check(stream)
+    assert ei.value.code == E_TIMEOUT
+    batch.close()
+    monkeypatch.delenv("PREC_GPU_BATCH_NEVER_SIGNAL")
+    monkeypatch.delenv("PREC_GPU_BATCH_SPIN_LIMIT")
+    batch = gpu.Batch(db.items())
+    db.out.fill_(-1)
+    batch.run(stream)
+    gpu.stream_check(stream)
+    for i in range(len(sizes)):
+        a, b = db.operands(i)
+        assert np.array_equal(db.result(i), O.mul_ntt(a, b)), (i, sizes[i])
+    batch.close()

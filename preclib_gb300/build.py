@@ -65,7 +65,7 @@ def build(verbose: bool = False, extra=()) -> str:
     return out
 
 
-PI_SOURCES = ("bignum.cpp", "pi_chudnovsky.cpp", "pi_kernels.cu", "dnat.cu")
+PI_SOURCES = ("bignum.cpp", "pi_chudnovsky.cpp", "pi_kernels.cu", "dnat.cu", "ddec.cu")
 PI_EXE = "pi_gb300"
 
 

@@ -404,10 +404,7 @@ Nat isqrt(const Nat& n) {
 namespace {
 
 constexpr u64 kTen19 = 10000000000000000000ull;  // 10^19 >= 2^63: a normalized divisor
-#ifndef PI_LEAF_DIGITS
-#define PI_LEAF_DIGITS 2048
-#endif
-constexpr size_t kLeafDigits = PI_LEAF_DIGITS;    // digits converted per leaf on the host
+constexpr size_t kLeafDigits = kDecimalLeafDigits;  // digits converted per leaf
 
 // a /= 10^19 in place, returns the remainder (2-by-1 division with the
 // precomputed inverse v = floor((2^128 - 1) / d) - 2^64)

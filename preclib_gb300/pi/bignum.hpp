@@ -112,6 +112,13 @@ Nat isqrt(const Nat& n);
 // (the Newton inverse square root isqrt is built on)
 Nat invsqrt(const Nat& n, size_t e, size_t p);
 
+// Digits per leaf of the decimal conversion (divide and conquer down to
+// numbers below 10^L, each then converted by repeated division by 10^19)
+#ifndef PI_LEAF_DIGITS
+#define PI_LEAF_DIGITS 2048
+#endif
+constexpr size_t kDecimalLeafDigits = PI_LEAF_DIGITS;
+
 // The powers 10^(L * 2^j), j < levels (L = the leaf size in digits), and
 // their reciprocals: all that decimal conversion needs besides x, so a
 // caller that knows the size of x can build them ahead of time.

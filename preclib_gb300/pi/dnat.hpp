@@ -17,6 +17,8 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 #include "bignum.hpp"
 
@@ -43,6 +45,13 @@ struct DNat {
     DNat& operator=(DNat&& o) noexcept;
     ~DNat();
     bool zero() const { return n == 0; }
+};
+
+// bignum.hpp's DecimalPowers on the device: pw[j] = 10^(L * 2^j), rx[j] its
+// reciprocal at precision P[j] = bitlen(pw[j]) + 34 (L = kDecimalLeafDigits)
+struct DevDecimalPowers {
+    std::vector<DNat> pw, rx;
+    std::vector<size_t> P;
 };
 
 class DevMath {
@@ -75,6 +84,16 @@ public:
 
     // bignum.hpp's Newton operations on device numbers (same contracts)
     DNat recip(const DNat& D, size_t p);
+    // the conversion's powers and reciprocals (bignum.hpp's decimal_powers)
+    DevDecimalPowers decimal_powers(int levels);
+    // powers made on another math object's stream, after it synchronised
+    void adopt(DevDecimalPowers& p);
+    // the decimal digits of x without leading zeros ("0" for zero), as
+    // bignum.hpp's to_decimal: the same divide and conquer on the powers
+    // (pw holds at least decimal_levels(digits of x) levels), every level's
+    // pieces split on the device in one pass, the leaves converted by one
+    // kernel; only the digit text comes back (ddec.cu)
+    std::string to_decimal(const DNat& x, const DevDecimalPowers& pw);
     void divmod_recip(const DNat& N, const DNat& D, const DNat& X, size_t P, DNat* q, DNat* r);
     DNat isqrt(const DNat& n);
 

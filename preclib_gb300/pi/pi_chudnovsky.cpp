@@ -690,11 +690,16 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
     const bool host_newton = hn && hn[0] == '1';
     Nat root;     // host-resident form
     DNat root_d;  // device-resident form
-    DecimalPowers pows;
+    DecimalPowers pows;     // host-resident form
+    DevDecimalPowers dpows; // device-resident form
     std::promise<void> root_set;
     std::future<void> root_ready = root_set.get_future();
-    // pi * 10^digits < 4 * 10^digits: at most digits + 1 decimal digits
+    // pi * 10^digits < 4 * 10^digits: at most digits + 1 decimal digits (the
+    // host form converts it); the device form converts pi * 10^(digits+10)
+    // before the division by 10^10 and drops the last 10 digits: at most
+    // digits + 12 by the conversion's bound on the digit count
     const int levels = decimal_levels(digits + 2);
+    const int dlevels = decimal_levels(digits + 12);
     std::thread side([&] {
         const double s0 = now_sec();
         if (host_newton) {
@@ -703,16 +708,26 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
             // 10005 * 10^(2 work) and its square root without leaving the device
             cudaStream_t sst = nullptr;
             check_cuda(cudaStreamCreateWithFlags(&sst, cudaStreamNonBlocking), "stream");
+            double s1 = 0;
             {
                 DevMath dm(sst);
                 const DNat n = dm.mul_u64(dm.pow_u64(10, 2 * work), 10005);
                 root_d = dm.isqrt(n);
                 check_cuda(cudaStreamSynchronize(sst), "square root");
+                root_d.st = nullptr;  // handed to the main thread (its stream adopts it)
+                s1 = now_sec();
+                root_set.set_value();
+                dpows = dm.decimal_powers(dlevels);
+                check_cuda(cudaStreamSynchronize(sst), "decimal powers");
+                for (DNat& x : dpows.pw) x.st = nullptr;
+                for (DNat& x : dpows.rx) x.st = nullptr;
                 dm_stats_add(dm);
             }
-            check_cuda(cudaStreamSynchronize(sst), "square root");
-            root_d.st = nullptr;  // handed to the main thread (its stream adopts it)
+            check_cuda(cudaStreamSynchronize(sst), "side stream");
             cudaStreamDestroy(sst);
+            ph.sqrt = s1 - s0;
+            ph.powers = now_sec() - s1;
+            return;
         }
         const double s1 = now_sec();
         root_set.set_value();
@@ -737,7 +752,8 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
     const size_t root_bits = (size_t)(std::log2(std::sqrt(10005.0)) + (double)work * std::log2(10.0)) + 2;
     const size_t P = bitlen(q426880) + root_bits - bitlen(T) + 2 + 32;
     Nat pi, rem;
-    double t2r = 0, t2 = 0;
+    std::string s;
+    double t2r = 0, t2 = 0, t3 = 0;
     if (host_newton) {
         const Nat X = recip(T, P);
         t2r = now_sec();
@@ -745,6 +761,10 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
         t2 = now_sec();
         const Nat num = mul(q426880, root);
         divmod_recip(num, T, X, P, pi, rem);
+        divmod_u64(pi, 10000000000ull);
+        t3 = now_sec();
+        side.join();
+        s = to_decimal(pi, 0, &pows);
     } else {
         // T, Q * 426880 up, the quotient down; everything between on the device
         DevMath dm(gpu_stream());
@@ -759,13 +779,16 @@ std::string pi_digits(size_t digits, Phases& ph, const std::function<void()>& de
         root_d = DNat();
         DNat pid, remd;
         dm.divmod_recip(num, Td, X, P, &pid, &remd);
-        pi = dm.download(pid);
+        t3 = now_sec();
+        // the digits of pi * 10^(digits + 10) on the device; dropping the
+        // last 10 is the floor division by 10^10
+        side.join();
+        dm.adopt(dpows);
+        s = dm.to_decimal(pid, dpows);
+        s = s.size() > 10 ? s.substr(0, s.size() - 10) : std::string("0");
+        dpows = DevDecimalPowers();
         dm_stats_add(dm);
     }
-    divmod_u64(pi, 10000000000ull);
-    double t3 = now_sec();
-    side.join();
-    std::string s = to_decimal(pi, 0, &pows);
     double t4 = now_sec();
     ph.split = t1 - t0;
     ph.root_wait = t2 - t2r;

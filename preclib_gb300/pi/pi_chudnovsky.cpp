@@ -23,8 +23,8 @@
 //   * the square root and the conversion's powers of ten (with their
 //     reciprocals) depend only on the digit count, so a second host thread
 //     computes them while the binary splitting and the division run.
-// The tree's four lowest levels (blocks of 16 terms, products of at most
-// about 20 limbs) and any other product of at most kHostMaxLimbs limbs run
+// The tree's five lowest levels (blocks of 32 terms, products of at most
+// about 66 limbs) and any other product of at most kHostMaxLimbs limbs run
 // on the host threads, as the reference multiplies such sizes with its
 // schoolbook and Karatsuba code; everything larger is computed by
 // libprecgpu.  There is no CPU path for those: without a device the
@@ -343,9 +343,14 @@ T* dev_alloc(size_t n) {
     return static_cast<T*>(p);
 }
 
-// A 16-term block on the stack: the node of terms [a, b) with fixed-size
-// magnitudes (no heap allocation), by the same recursive halving.
-constexpr int kSmallLimbs = 48;  // bound of P, Q, |T| of 16 terms (about 36 limbs)
+// A block of kHostBlock terms on the stack: the node of terms [a, b) with
+// fixed-size magnitudes (no heap allocation), by the same recursive
+// halving.  For terms k < 3.1e7 (the program's limit of 4.3e8 digits) a
+// term's q_k has at most 128 bits, p_k 81 and |t_k| 135, so a block of b
+// terms has Q, P and |T| below 2^(128 (b - 1) + 140): 65 limbs for 32
+// terms, and nothing inside it (Tl * Qr of two 16-term halves, plus the
+// sum) above 66.
+constexpr int kSmallLimbs = 72;
 
 struct SmallNat {
     uint32_t n = 0;
@@ -451,24 +456,27 @@ void small_split(u64 a, u64 b, SmallNode& out) {
 // runs while the device comes up.
 struct HostBlocks {
     DevLevel L;  // offsets and sizes (no device buffers yet)
-    std::vector<u64> hv;
+    // limbs in fixed slots; the tails past each number's size are never read
+    // (not zero-filled: that took longer than the blocks' arithmetic)
+    std::unique_ptr<u64[]> hv;
+    size_t hv_n = 0;
     std::vector<int8_t> hs;
 };
 
 HostBlocks host_blocks(size_t terms, size_t block) {
     HostBlocks B;
     DevLevel& L = B.L;
-    std::vector<u64>& hv = B.hv;
     std::vector<int8_t>& hs = B.hs;
     const size_t m = (terms + block - 1) / block;
     constexpr size_t slot = 3 * kSmallLimbs;
     L.op.resize(m), L.oq.resize(m), L.ot.resize(m), L.np.resize(m), L.nq.resize(m), L.nt.resize(m);
-    hv.resize(m * slot);
+    B.hv_n = m * slot;
+    B.hv.reset(new u64[B.hv_n]);
     hs.resize(m);
     parallel_for(m, [&](size_t i) {
         SmallNode nd;
         small_split(i * block, std::min<size_t>(terms, (i + 1) * block), nd);
-        u64* h = hv.data() + i * slot;
+        u64* h = B.hv.get() + i * slot;
         std::copy(nd.p.d, nd.p.d + nd.p.n, h);
         std::copy(nd.q.d, nd.q.d + nd.q.n, h + kSmallLimbs);
         std::copy(nd.t.d, nd.t.d + nd.t.n, h + 2 * kSmallLimbs);
@@ -481,9 +489,9 @@ HostBlocks host_blocks(size_t terms, size_t block) {
 
 void upload_blocks(HostBlocks& B, DevLevel& L, cudaStream_t st) {
     L = std::move(B.L);
-    L.buf = dev_alloc<u64>(B.hv.size());
+    L.buf = dev_alloc<u64>(B.hv_n);
     L.sign = dev_alloc<int8_t>(B.hs.size());
-    check_cuda(cudaMemcpyAsync(L.buf, B.hv.data(), B.hv.size() * sizeof(u64), cudaMemcpyHostToDevice, st),
+    check_cuda(cudaMemcpyAsync(L.buf, B.hv.get(), B.hv_n * sizeof(u64), cudaMemcpyHostToDevice, st),
                "level upload");
     check_cuda(cudaMemcpyAsync(L.sign, B.hs.data(), B.hs.size(), cudaMemcpyHostToDevice, st), "sign upload");
     check_cuda(cudaStreamSynchronize(st), "level upload");
@@ -501,9 +509,14 @@ Nat download(const uint64_t* d, size_t n, cudaStream_t st) {
 bool trace_on();
 Node host_split(u64 a, u64 b);
 
-constexpr size_t kHostBlock = 16;
+// 32 terms: the host threads compute the tree's five lowest levels while the
+// device comes up (its context takes ~0.2 s); at 10^8 digits the device had
+// spent 0.076 s on the fifth level (9e5 products of ~30 limbs), mostly in
+// planning and descriptor traffic.  (64-term blocks measured no faster: the
+// host blocks took 0.145 s instead of 0.09.)
+constexpr size_t kHostBlock = 32;
 
-// Q(0, terms) and T(0, terms) from the host blocks of 16 terms: every level
+// Q(0, terms) and T(0, terms) from the host blocks of kHostBlock terms: every level
 // on the device (products through one batch per level, T's signed sums by
 // signed_add_many); only the root comes back.
 void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
@@ -614,7 +627,7 @@ void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
 // Q(0, terms) and T(0, terms)
 void binary_split(size_t terms, Nat& Q, Nat& T, bool& tneg) {
     // the lowest levels in blocks of kHostBlock terms on the host threads:
-    // their products have at most about 20 limbs
+    // their products have at most about 66 limbs
     double t0 = now_sec();
     std::vector<Node> lv((terms + kHostBlock - 1) / kHostBlock);
     parallel_for(lv.size(), [&](size_t i) {

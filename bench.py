@@ -417,7 +417,7 @@ def run_ours(args):
         sus = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(64)]
         sus_ms = []
         t_sus = time.perf_counter()
-        while time.perf_counter() - t_sus < SUSTAIN_S:
+        while time.perf_counter() - t_sus < args.sustain:
             for j, (e0, e1) in enumerate(sus):
                 e0.record(stream)
                 step()
@@ -531,7 +531,7 @@ def run_ours(args):
             "clocks_window": "the %d timed steps, then the same step back to back for %.2f s "
                              "(sustained)" % (args.steps, sus_s),
             "sustained": {"seconds": round(sus_s, 3), "products": len(sus_ms),
-                          "median_ms": round(statistics.median(sus_ms), 4)},
+                          "median_ms": round(statistics.median(sus_ms), 4) if sus_ms else None},
             "cpu_baseline": cpu,
         }
         if subs:
@@ -893,6 +893,9 @@ def main():
                          "serve: serving loop under Poisson arrivals; pi: pi to 10^8 digits; "
                          "fft: 3000 x 3000 limbs on the FP64 band")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
+    ap.add_argument("--sustain", type=float, default=SUSTAIN_S,
+                    help="seconds of back-to-back products after the timed steps, for the clock sampler "
+                         "(0 for profiling runs)")
     ap.add_argument("--headline-only", action="store_true",
                     help="default workload: omit the other configurations' sub-results")
     args = ap.parse_args()

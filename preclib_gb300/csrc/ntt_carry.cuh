@@ -31,8 +31,6 @@ __device__ __forceinline__ uint32_t ld_work(const uint32_t* p) {
     else return *p;
 }
 
-constexpr int kBlockLimbs = kCarryThreads * kCarryLimbs;
-
 // ---- set 2: one coefficient per 64-bit limb
 
 // a coefficient c < p1..p5 < 2^150 as three words (w2 < 2^22)
@@ -102,9 +100,12 @@ struct WideEdge {
 };
 
 // T[k] = S_(m0+k) for this thread's limbs and hi(S_(m0-1)); the words the
-// first limbs need from below come from the lane below, from the warp
-// below (shared memory), or for the block's first thread from three
-// coefficients computed again by lanes 0..2 of warp 0.
+// first limbs need from below come from the lane below or, for a warp's
+// lane 0, from the warp below (shared memory).  The block's thread 0 holds
+// the four coefficients just below the block's first limb and outputs
+// nothing, so every thread recombines exactly four coefficients (three lanes
+// of warp 0 recomputing the block's edge after their own four kept the
+// other warps waiting at the barrier: 3.9 stalled warps per issue).
 template <bool LAZY>
 __device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& args, int64_t m0, u128 (&T)[kCarryLimbs],
                                           uint64_t& prev_hi, WideEdge* s_edge) {
@@ -113,7 +114,7 @@ __device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& ar
     const uint64_t N = 1ull << args.k;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     Coef3 c[L];
-    if ((uint64_t)m0 + L <= N) {
+    if (m0 >= 0 && (uint64_t)m0 + L <= N) {  // (block 0's thread 0 starts at -4)
 #pragma unroll
         for (int h = 0; h < L / 4; ++h) {
             uint4 r[5];
@@ -146,24 +147,6 @@ __device__ __forceinline__ void wide_sums(const ProdPtrs& PP, const ProdArgs& ar
     uint32_t w2m2 = __shfl_up_sync(0xffffffffu, c[L - 2].w2, 1);
     uint32_t him1 = __shfl_up_sync(0xffffffffu, hi_last, 1);
     if (lane == 31) s_edge[warp] = WideEdge{c[L - 1].w1, c[L - 1].w2, c[L - 2].w2, hi_last};
-    if (warp == 0) {
-        // the block's first limb: coefficients m0-1, m0-2, m0-3 (lanes 0, 1, 2)
-        Coef3 e = Coef3{0, 0, 0};
-        const int64_t mb = m0 - lane * L;  // the block's first limb
-        if (lane < 3) e = coef5<LAZY>(PP.work, N, mb - 1 - lane, args);
-        const uint64_t e1w0 = __shfl_sync(0xffffffffu, e.w0, 0);
-        const uint64_t e1w1 = __shfl_sync(0xffffffffu, e.w1, 0);
-        const uint32_t e1w2 = __shfl_sync(0xffffffffu, e.w2, 0);
-        const uint64_t e2w1 = __shfl_sync(0xffffffffu, e.w1, 1);
-        const uint32_t e2w2 = __shfl_sync(0xffffffffu, e.w2, 1);
-        const uint32_t e3w2 = __shfl_sync(0xffffffffu, e.w2, 2);
-        if (lane == 0) {
-            w1m1 = e1w1;
-            w2m1 = e1w2;
-            w2m2 = e2w2;
-            him1 = (uint32_t)(((u128)e1w0 + e2w1 + e3w2) >> 64);
-        }
-    }
     __syncthreads();
     if (lane == 0 && warp > 0) {
         const WideEdge e = s_edge[warp - 1];
@@ -195,7 +178,10 @@ __device__ __forceinline__ void crt_carry_tile(const ProdArgs& args, const ProdP
     if ((int)bid >= PP.nblk) return;  // batch: a shorter product of the class
     const uint64_t N = 1ull << args.k;
     const int lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)bid * kBlockLimbs + threadIdx.x * kCarryLimbs;
+    constexpr int BL = crt_block_limbs(SET);  // limbs the block outputs
+    // 64-bit digits: thread 0 takes the four coefficients below the block
+    const int64_t m0 = (int64_t)bid * BL + ((int)threadIdx.x - (set_wide(SET) ? 1 : 0)) * kCarryLimbs;
+    const bool edge_only = set_wide(SET) && threadIdx.x == 0;
 
     u128 T[kCarryLimbs];
     uint64_t prev_hi = 0;
@@ -255,11 +241,12 @@ __device__ __forceinline__ void crt_carry_tile(const ProdArgs& args, const ProdP
     uint32_t gbits;
     bool G, P;
     limbs_from_sums<kCarryLimbs>(T, prev_hi, v, gbits, G, P);
+    if (edge_only) G = false, P = true;  // no limbs: the identity of the carry scan
 
     uint32_t* agg = PP.scratch + 1;
     auto publish = [&](bool Gb, bool Pb) { agg[bid] = (Gb ? 1u : 0u) | (Pb ? 2u : 0u); };
     const bool cin = block_carry_in0(G, P, sh, publish);
-    limbs_finish<kCarryLimbs>(m0, PP.lout, v, gbits, cin, PP.out);
+    if (!edge_only) limbs_finish<kCarryLimbs>(m0, PP.lout, v, gbits, cin, PP.out);
 
     // ---- phase 2: the last block resolves the carries between blocks.
     // The barrier orders every thread's limb and aggregate stores before
@@ -305,8 +292,8 @@ __device__ __forceinline__ void crt_carry_tile(const ProdArgs& args, const ProdP
     auto enter = [&](int b, uint32_t a) {
         if (c) {
             // the carry enters block b: +1 ripples through its all-ones limbs
-            const uint64_t lim_end = min((uint64_t)(b + 1) * kBlockLimbs, PP.lout);
-            for (uint64_t m = (uint64_t)b * kBlockLimbs; m < lim_end; ++m) {
+            const uint64_t lim_end = min((uint64_t)(b + 1) * BL, PP.lout);
+            for (uint64_t m = (uint64_t)b * BL; m < lim_end; ++m) {
                 const uint64_t x = __ldcg(&PP.out[m]) + 1;
                 PP.out[m] = x;
                 if (x != 0) break;

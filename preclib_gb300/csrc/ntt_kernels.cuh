@@ -162,6 +162,15 @@ constexpr int kCarryThreads = 256;
 #define PREC_COL_GROUP 8
 #endif
 constexpr int kCarryLimbs = PREC_CARRY_LIMBS;  // limbs per thread in the carry kernel
+// limbs one CRT/carry block outputs: kCarryThreads * kCarryLimbs for the
+// 32-bit-digit sets; the 64-bit-digit sets' blocks give their first thread
+// the coefficients just below the block (it outputs no limbs), one thread's
+// worth fewer
+constexpr int kCarryBlockLimbs = kCarryThreads * kCarryLimbs;
+constexpr int kWideCarryBlockLimbs = kCarryBlockLimbs - kCarryLimbs;
+__host__ __device__ constexpr int crt_block_limbs(int set) {
+    return set_wide(set) ? kWideCarryBlockLimbs : kCarryBlockLimbs;
+}
 constexpr int kColGroup = PREC_COL_GROUP;      // adjacent columns per column-pass CTA (4 when N1 = 2^13)
 
 // Explicit graph construction.  While a thread has a recorder installed,

@@ -239,7 +239,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             // a product of 2^k points has at most 2^(k-1) + 1 limbs on 32-bit
             // digits, 2^k + 1 on 64-bit digits
             const uint64_t lout_max = set_wide(c.pl.set) ? (1ull << c.k) + 1 : (1ull << c.k) / 2 + 1;
-            const size_t carry_words = (size_t)(lout_max / (kCarryThreads * kCarryLimbs)) + 2;
+            const size_t carry_words = (size_t)(lout_max / crt_block_limbs(c.pl.set)) + 2;
             c.ws_per = align256(((size_t)2 * c.pl.nprimes << c.k) * sizeof(uint32_t) + carry_words * sizeof(uint32_t));
             c.per_chunk = (int)std::min<size_t>({n, std::max<size_t>(1, budget / c.ws_per), 65535});
             ws_off.push_back(bytes);
@@ -289,7 +289,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             c.ws = base + ws_off[ci];
             if (c.persistent) c.sched = reinterpret_cast<uint32_t*>(base + sched_off[ci]);
             std::vector<ProdPtrs> h(n);
-            const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+            const uint64_t bl = (uint64_t)crt_block_limbs(c.pl.set);
             for (size_t j = 0; j < n; ++j) {
                 const prec_gpu_product_t& p = items[c.items[j]];
                 ProdPtrs& d = h[j];

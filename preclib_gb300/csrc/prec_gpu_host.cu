@@ -238,7 +238,7 @@ int plan_for(uint64_t da, uint64_t db, uint64_t lout, Plan& pl, bool wide) {
         }
     }
     apply_config(pl, config_for(k, pl.set));
-    const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+    const uint64_t bl = (uint64_t)crt_block_limbs(pl.set);
     pl.nblk = (int)((lout + bl - 1) / bl);
     pl.work_bytes = ((size_t)2 * pl.nprimes << k) * sizeof(uint32_t) + ((size_t)pl.nblk + 1) * sizeof(uint32_t);
     return 0;
@@ -716,7 +716,7 @@ static int enqueue_graph(Lane& L, const ProdArgs& args, const Plan& pl, cudaStre
         cls.out = nullptr;
         cls.work = cls.scratch = nullptr;
         const uint64_t lout_max = set_wide(pl.set) ? (1ull << pl.k) + 1 : (1ull << pl.k) / 2 + 1;
-        const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+        const uint64_t bl = (uint64_t)crt_block_limbs(pl.set);
         const int max_nblk = (int)((lout_max + bl - 1) / bl);
         // the four launches as a chain of kernel nodes (explicit
         // construction: no stream capture)
@@ -1057,7 +1057,7 @@ static int host_mul(const uint64_t* a, size_t an, const uint64_t* b, size_t bn, 
         if ((r = enqueue_ntt(c, L, d_a, la, d_b, lb, d_out, pl, st, L.d_err, nullptr, L.ev_a, L.ev_b, chunked ? &ch : nullptr)))
             return r;
         if (chunked) {
-            const uint64_t bl = (uint64_t)kCarryThreads * kCarryLimbs;
+            const uint64_t bl = (uint64_t)crt_block_limbs(pl.set);
             for (int i = 0; i < ch.count; ++i) {
                 const uint64_t lo = std::min((uint64_t)ch.blk0[i] * bl, lout);
                 const uint64_t hi = std::min((uint64_t)ch.blk0[i + 1] * bl, lout);

@@ -1,6 +1,7 @@
 // pi_chudnovsky.cpp -- pi by the Chudnovsky series on the GB300 multiply.
 //
 //   pi_gb300 DIGITS [--phases] [--full] [--file PATH]
+//   pi_gb300 --self-check
 //
 // Same computation and output as preclib's pi/pi_chudnovsky.cpp (same
 // guard digits, term count, scaled square root, floor divisions, decimal
@@ -818,6 +819,91 @@ std::string short_form(const std::string& s, bool full) {
     return s.substr(0, 11) + "..." + s.substr(s.size() - 10);
 }
 
+// --self-check: the device-resident forms of the decimal conversion, the
+// square root and the exact division (ddec.cu, dnat.cu) against bignum.cpp's
+// host-resident forms, on the numbers where a divide and conquer or a
+// correction step goes wrong first: zero, the powers of ten at the leaf and
+// level sizes and their neighbours, long runs of nines and zeros, all-ones
+// limbs, perfect squares and their predecessors, random numbers.  Returns the
+// number of disagreements.
+int self_check() {
+    DevMath dm(gpu_stream());
+    int bad = 0;
+    auto report = [&](const std::string& what, bool ok) {
+        if (!ok) {
+            ++bad;
+            std::fprintf(stderr, "self-check: %s: device and host forms differ\n", what.c_str());
+        }
+    };
+    u64 rs = 0x9E3779B97F4A7C15ull;
+    auto random_nat = [&](size_t limbs) {
+        Nat x;
+        x.d.resize(limbs);
+        for (u64& v : x.d) {  // xorshift64
+            rs ^= rs << 13, rs ^= rs >> 7, rs ^= rs << 17;
+            v = rs;
+        }
+        normalize(x);
+        return x;
+    };
+    const Nat one(1);
+    const Nat t2048 = pow_u64(10, kDecimalLeafDigits), t4096 = sqr(t2048), t8192 = sqr(t4096);
+    std::vector<std::pair<std::string, Nat>> xs;
+    xs.push_back({"0", Nat()});
+    xs.push_back({"1", one});
+    xs.push_back({"9", Nat(9)});
+    for (const auto& p : {std::make_pair(std::string("10^2048"), &t2048), std::make_pair(std::string("10^4096"), &t4096),
+                          std::make_pair(std::string("10^8192"), &t8192)}) {
+        xs.push_back({p.first + " - 1", sub(*p.second, one)});
+        xs.push_back({p.first, *p.second});
+        xs.push_back({p.first + " + 1", add(*p.second, one)});
+    }
+    const Nat t50000 = pow_u64(10, 50000);
+    xs.push_back({"(10^50000 - 1) 10^50000", mul(sub(t50000, one), t50000)});
+    xs.push_back({"2^64000 - 1", sub(pow2(64000), one)});
+    xs.push_back({"2^(64 * 50000) - 1", sub(pow2(64 * 50000), one)});
+    xs.push_back({"random 5190 limbs", random_nat(5190)});
+    xs.push_back({"random 51906 limbs", random_nat(51906)});
+    int levels = 0;
+    for (const auto& x : xs) levels = std::max(levels, decimal_levels((size_t)((double)bitlen(x.second) * 0.30103) + 2));
+    DevDecimalPowers pw = dm.decimal_powers(levels);
+    for (const auto& x : xs) {
+        const std::string h = to_decimal(x.second, 0);
+        const std::string d = dm.to_decimal(dm.upload(x.second), pw);
+        report("decimal text of " + x.first, h == d);
+    }
+    // square roots: the pi program's kind, perfect squares and their neighbours, random
+    const Nat s = random_nat(40000);
+    const Nat s2 = sqr(s);
+    std::vector<std::pair<std::string, Nat>> ns;
+    ns.push_back({"10005 10^100000", mul_u64(pow_u64(10, 100000), 10005)});
+    ns.push_back({"s^2", s2});
+    ns.push_back({"s^2 - 1", sub(s2, one)});
+    ns.push_back({"s^2 + 2s", add(s2, shl(s, 1))});
+    ns.push_back({"random 300000 limbs", random_nat(300000)});
+    for (const auto& n : ns) report("square root of " + n.first, cmp(isqrt(n.second), dm.download(dm.isqrt(dm.upload(n.second)))) == 0);
+    // exact division: random, and quotients at the correction's edges
+    const Nat D = random_nat(150000);
+    const Nat q0 = random_nat(250000);
+    std::vector<std::pair<std::string, Nat>> nums;
+    nums.push_back({"random 400000 limbs", random_nat(400000)});
+    nums.push_back({"q D", mul(q0, D)});
+    nums.push_back({"q D - 1", sub(mul(q0, D), one)});
+    nums.push_back({"q D + D - 1", sub(add(mul(q0, D), D), one)});
+    const DNat Dd = dm.upload(D);
+    for (const auto& n : nums) {
+        const size_t P = bitlen(n.second) - bitlen(D) + 2 + 32;
+        Nat hq, hr;
+        divmod_recip(n.second, D, recip(D, P), P, hq, hr);
+        DNat dq, dr;
+        dm.divmod_recip(dm.upload(n.second), Dd, dm.recip(Dd, P), P, &dq, &dr);
+        report("division of " + n.first, cmp(hq, dm.download(dq)) == 0 && cmp(hr, dm.download(dr)) == 0);
+    }
+    std::fprintf(stderr, "self-check: %zu conversions, %zu square roots, %zu divisions, %d disagreements\n",
+                 xs.size(), ns.size(), nums.size(), bad);
+    return bad;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -831,6 +917,15 @@ int main(int argc, char** argv) {
     size_t digits = 100;
     bool phases = false, full = false;
     std::string file;
+    if (argc > 1 && std::string(argv[1]) == "--self-check") {
+        const int rc = prec_gpu_init(-1);
+        if (rc) die("prec_gpu_init", rc);
+        GpuBackend be;
+        set_backend(&be);
+        const int bad = self_check();
+        set_backend(nullptr);
+        return bad ? 1 : 0;
+    }
     if (argc > 1) digits = (size_t)std::strtoull(argv[1], nullptr, 10);
     for (int i = 2; i < argc; ++i) {
         const std::string a = argv[i];

@@ -56,6 +56,9 @@ def main():
     recs.append(record("cfg1_8192x8192_ntt", dict(kind="splitmix64", seed_a=1, seed_b=2, an=8192, bn=8192), "ntt"))
     recs.append(record("cfg2_1Mx1M_ntt", dict(kind="splitmix64", seed_a=3, seed_b=4, an=1 << 20, bn=1 << 20), "ntt"))
     recs.append(record("cfg2_3000x3000_fft", dict(kind="splitmix64", seed_a=5, seed_b=6, an=3000, bn=3000), "fft"))
+    # above 1M x 1M: the 64-bit-digit plan over the second five-prime set
+    # (2^23 points), the largest requests of the serving configuration
+    recs.append(record("big_4Mx4M_ntt", dict(kind="splitmix64", seed_a=25, seed_b=26, an=1 << 22, bn=1 << 22), "ntt"))
     # test/bench_ntt.cpp sizes (1024..65536 limbs, seeds 1000+n, 2000+n)
     n = 1024
     while n <= 65536:

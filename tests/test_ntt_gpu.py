@@ -146,6 +146,22 @@ def test_1m_golden(gpu, golden):
             gpu.set_wide_digits(prev)
 
 
+def test_4m_golden(gpu, golden):
+    """The 4M x 4M product against the reference's own digest on both digit
+    widths: 2^23 points over the second five-prime set (64-bit digits, the
+    default) and 2^24 points over the reference's three primes (32-bit)."""
+    rec = [r for r in golden if r["name"] == "big_4Mx4M_ntt"][0]
+    a, b = patterns.make(rec["gen"])
+    for wide, k in ((True, 23), (False, 24)):
+        prev = gpu.set_wide_digits(wide)
+        try:
+            assert _digest(gpu.mul(a, b, ntt=True)) == rec["sha256"], wide
+            st = gpu.last_stats()
+            assert st.log2_n == k and st.path == 1
+        finally:
+            gpu.set_wide_digits(prev)
+
+
 def test_device_api_matches_host_api(gpu):
     torch = pytest.importorskip("torch")
     for (an, bn) in ((5000, 4000), (1 << 18, 1 << 18), (50, 60)):

@@ -16,8 +16,12 @@ def _digest(out):
 
 def test_golden_vectors(golden):
     """Every reference-generated product is reproduced bit-exactly, and the
-    FFT restatement reproduces the reference's rounding distances."""
+    FFT restatement reproduces the reference's rounding distances.  (The
+    4M x 4M record, 12 s of oracle time, is pinned on the GPU path only:
+    test_ntt_gpu.py.)"""
     for rec in golden:
+        if rec["limbs"] > (1 << 21) + 2:
+            continue
         a, b = patterns.make(rec["gen"])
         if rec["ref_fn"] == "sqr":
             out = O.mul_ntt(a, a)  # an exact square, whichever band made it

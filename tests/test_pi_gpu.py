@@ -44,3 +44,15 @@ def test_pi_digits_host_newton(gpu, tmp_path):
     assert r.returncode == 0, r.stderr
     data = out.read_bytes()
     assert hashlib.sha256(data).hexdigest() == want["sha256"]
+
+
+def test_pi_device_forms_match_host_forms(gpu):
+    """pi_gb300 --self-check: the device-resident decimal conversion, square
+    root and exact division agree with the host-resident forms of
+    bignum.cpp on zero, powers of ten at the conversion's leaf and level
+    sizes and their neighbours, runs of nines and zeros, all-ones limbs,
+    perfect squares and their neighbours, quotients at the correction's edges
+    and random numbers."""
+    r = subprocess.run([EXE, "--self-check"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "0 disagreements" in r.stderr, r.stderr

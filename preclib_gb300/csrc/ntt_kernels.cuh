@@ -143,7 +143,8 @@ struct SmallDesc {
     uint64_t la, lb, lout;
     int k;
     int square;  // a == b (the single-CTA kernel reads the operand twice)
-    CrtConst crt;
+    // (the length's CRT constants are a kernel argument: one copy per launch,
+    // not one per product of a batch class)
 };
 
 // device error bits
@@ -228,7 +229,7 @@ void uncount_launches(uint64_t n);
 size_t ntt_small_smem_bytes(int k);
 int ntt_small_threads(int k);
 void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k,
-                      const FieldArgs& f, cudaStream_t st, cudaEvent_t* ev = nullptr);
+                      const FieldArgs& f, const CrtConst& crt, cudaStream_t st, cudaEvent_t* ev = nullptr);
 // Side streams of a single product: each prime's transform kernels run as
 // an independent chain (fork from and join to the caller's stream), so
 // one prime's tail wave overlaps another prime's work.

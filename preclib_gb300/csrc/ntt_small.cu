@@ -19,7 +19,8 @@ __device__ __forceinline__ u128 small_coef(const uint32_t* sm, int64_t i, const 
 }
 
 template <int M>
-__global__ void __launch_bounds__(256) k_small(const SmallDesc* __restrict__ descs, SmallDesc single, FieldArgs f) {
+__global__ void __launch_bounds__(256) k_small(const SmallDesc* __restrict__ descs, SmallDesc single, FieldArgs f,
+                                               CrtConst crt) {
     extern __shared__ uint32_t sm[];
     __shared__ BlockCarryShared sh;
     constexpr int NP = sch_np(M);
@@ -122,10 +123,10 @@ __global__ void __launch_bounds__(256) k_small(const SmallDesc* __restrict__ des
         u128 T[L];
 #pragma unroll
         for (int k = 0; k < L; ++k)
-            T[k] = small_coef<M>(sm, 2 * (m0 + k), d.crt, f) + (small_coef<M>(sm, 2 * (m0 + k) + 1, d.crt, f) << 32);
+            T[k] = small_coef<M>(sm, 2 * (m0 + k), crt, f) + (small_coef<M>(sm, 2 * (m0 + k) + 1, crt, f) << 32);
         uint64_t prev_hi = 0;
         if (m0 > 0) {
-            const u128 tp = small_coef<M>(sm, 2 * m0 - 2, d.crt, f) + (small_coef<M>(sm, 2 * m0 - 1, d.crt, f) << 32);
+            const u128 tp = small_coef<M>(sm, 2 * m0 - 2, crt, f) + (small_coef<M>(sm, 2 * m0 - 1, crt, f) << 32);
             prev_hi = (uint64_t)(tp >> 64);
         }
         uint64_t v[L];
@@ -156,7 +157,7 @@ int ntt_small_threads(int k) {
 #define PREC_SMALL(X) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
 
 void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int count, int k, const FieldArgs& f,
-                      cudaStream_t st, cudaEvent_t* ev) {
+                      const CrtConst& crt, cudaStream_t st, cudaEvent_t* ev) {
     SmallDesc one{};
     if (single) one = *single;
     if (ev) cudaEventRecord(ev[0], st);
@@ -164,7 +165,7 @@ void ntt_launch_small(const SmallDesc* d_descs, const SmallDesc* single, int cou
     const size_t smem = ntt_small_smem_bytes(k);
 #define X(MM) \
     if (k == MM) {                                                     \
-        launch_kernel(k_small<MM>, count, threads, smem, st, d_descs, one, f); \
+        launch_kernel(k_small<MM>, count, threads, smem, st, d_descs, one, f, crt); \
         count_launches(1);                                             \
     }
     PREC_SMALL(X)

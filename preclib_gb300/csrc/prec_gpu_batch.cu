@@ -22,7 +22,6 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
-#include <map>
 #include <mutex>
 #include <vector>
 
@@ -127,7 +126,7 @@ static void batch_enqueue(prec_gpu_batch* b, cudaStream_t origin, bool branch) {
         cudaStream_t st = branch ? c.stream : origin;
         if (branch && !rec) cudaStreamWaitEvent(st, b->fork, 0);
         if (c.pl.path == 0) {
-            ntt_launch_small(c.d_small, nullptr, (int)c.items.size(), c.k, ctx_field(0), st);
+            ntt_launch_small(c.d_small, nullptr, (int)c.items.size(), c.k, ctx_field(0), c.pl.crt, st);
         } else {
             ProdArgs args{};
             args.err = b->err;
@@ -176,7 +175,10 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
     b->oneshot = ost;
     b->items.assign(items, items + count);
     b->err = ctx_device_err();
-    std::map<int, Cls> by_k;  // key: 64-bit digits << 8 | k << 1 | square
+    // classes by key (64-bit digits << 8 | k << 1 | square): a dense table,
+    // not a map lookup per product (a binary-splitting level has ~10^6 of them)
+    std::vector<int> cls_of(1 << 9, -1);
+    std::vector<Cls> found;
     const bool wide = wide_digits();
     for (size_t i = 0; i < count; ++i) {
         const prec_gpu_product_t& p = items[i];
@@ -201,7 +203,12 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
         const int kw = wide ? wide_log2(p.an, p.bn, k) : 0;
         if (kw) k = kw;
         const int sq = (p.a == p.b && p.an == p.bn && k > kSmallMaxLog2) ? 1 : 0;
-        Cls& c = by_k[(kw ? 1 << 8 : 0) | k << 1 | sq];
+        int& ci = cls_of[(kw ? 1 << 8 : 0) | k << 1 | sq];
+        if (ci < 0) {
+            ci = (int)found.size();
+            found.emplace_back();
+        }
+        Cls& c = found[ci];
         if (c.items.empty()) {
             if ((r = plan_for(2 * (uint64_t)p.an, 2 * (uint64_t)p.bn, p.an + p.bn, c.pl, wide))) {
                 batch_free(b);
@@ -230,8 +237,9 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
     std::vector<size_t> sched_off;
     size_t bytes = 0;
     std::vector<size_t> desc_off, ws_off;
-    for (auto& kv : by_k) {
-        Cls& c = kv.second;
+    for (int ci : cls_of) {
+        if (ci < 0) continue;  // key order, as before
+        Cls& c = found[ci];
         const size_t n = c.items.size();
         desc_off.push_back(bytes);
         bytes += align256(n * (c.pl.path == 0 ? sizeof(SmallDesc) : sizeof(ProdPtrs)));
@@ -251,7 +259,7 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
             ws_off.push_back(0);
             sched_off.push_back(0);
         }
-        b->classes.push_back(c);
+        b->classes.push_back(std::move(c));
     }
     b->d_bytes = bytes;
     if (bytes && oneshot) {
@@ -281,7 +289,6 @@ static int batch_build(const prec_gpu_product_t* items, size_t count, bool onesh
                 d.lout = p.an + p.bn;
                 d.k = c.k;
                 d.square = p.a == p.b && p.an == p.bn;
-                d.crt = c.pl.crt;
             }
             c.d_small = reinterpret_cast<SmallDesc*>(base + desc_off[ci]);
             BCK(upload(c.d_small, h.data(), n * sizeof(SmallDesc)));

@@ -783,8 +783,7 @@ static int enqueue_ntt(Ctx& c, Lane& L, const uint64_t* d_a, uint64_t la, const 
         d.lout = lout;
         d.k = pl.k;
         d.square = square;
-        d.crt = pl.crt;
-        ntt_launch_small(nullptr, &d, 1, pl.k, c.field[0], st, ev);
+        ntt_launch_small(nullptr, &d, 1, pl.k, c.field[0], pl.crt, st, ev);
     } else {
         ProdArgs args{};
         args.a = d_a;

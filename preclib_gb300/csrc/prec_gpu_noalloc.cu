@@ -247,8 +247,7 @@ extern "C" int prec_gpu_mul_device_noalloc(const uint64_t* d_a, size_t an, const
         s.lb = bn;
         s.lout = lout;
         s.k = k;
-        s.crt = na_crt(k);
-        ntt_launch_small(nullptr, &s, 1, k, d->field, st);
+        ntt_launch_small(nullptr, &s, 1, k, d->field, na_crt(k), st);
     } else {
         ProdArgs args{};
         args.a = d_a;

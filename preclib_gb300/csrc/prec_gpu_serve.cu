@@ -103,8 +103,7 @@ static int launch_request(prec_gpu_server* s, Slot& sl) {
         d.lb = p.bn;
         d.lout = p.an + p.bn;
         d.k = r.pl.k;
-        d.crt = r.pl.crt;
-        ntt_launch_small(nullptr, &d, 1, r.pl.k, ctx_field(0), st);
+        ntt_launch_small(nullptr, &d, 1, r.pl.k, ctx_field(0), r.pl.crt, st);
     } else {
         void* ws = nullptr;
         cudaError_t e = cudaMallocFromPoolAsync(&ws, r.bytes, s->pool, st);

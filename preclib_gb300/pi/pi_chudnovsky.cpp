@@ -101,6 +101,17 @@ static void dm_stats_add(const DevMath& dm) {
 }
 
 static cudaStream_t g_stream = nullptr;  // the main thread's stream (the backend's)
+
+// the device's default memory pool keeps freed memory for reuse (stream-
+// ordered allocations of the tree levels and the device-resident numbers)
+static void keep_pool_memory() {
+    int dev = 0;
+    cudaMemPool_t pool = nullptr;
+    check_cuda(cudaGetDevice(&dev), "device");
+    check_cuda(cudaDeviceGetDefaultMemPool(&pool, dev), "memory pool");
+    uint64_t keep = ~0ull;
+    check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "memory pool");
+}
 static cudaStream_t gpu_stream() { return g_stream; }
 
 struct GpuBackend : MulBackend {
@@ -327,9 +338,9 @@ struct DevLevel {
     uint64_t* buf = nullptr;
     int8_t* sign = nullptr;
     size_t nodes() const { return nq.size(); }
-    void release() {
-        if (buf) cudaFree(buf);
-        if (sign) cudaFree(sign);
+    void release(cudaStream_t st) {
+        if (buf) cudaFreeAsync(buf, st);
+        if (sign) cudaFreeAsync(sign, st);
         buf = nullptr;
         sign = nullptr;
     }
@@ -337,10 +348,13 @@ struct DevLevel {
 
 size_t up4(size_t x) { return (x + 3) & ~(size_t)3; }
 
+// stream-ordered, from the device's default pool (its release threshold
+// raised at start-up, so freed levels are reused without device-wide
+// synchronisation)
 template <class T>
-T* dev_alloc(size_t n) {
+T* dev_alloc(size_t n, cudaStream_t st) {
     void* p = nullptr;
-    check_cuda(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "device level buffer");
+    check_cuda(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), st), "device level buffer");
     return static_cast<T*>(p);
 }
 
@@ -490,8 +504,8 @@ HostBlocks host_blocks(size_t terms, size_t block) {
 
 void upload_blocks(HostBlocks& B, DevLevel& L, cudaStream_t st) {
     L = std::move(B.L);
-    L.buf = dev_alloc<u64>(B.hv_n);
-    L.sign = dev_alloc<int8_t>(B.hs.size());
+    L.buf = dev_alloc<u64>(B.hv_n, st);
+    L.sign = dev_alloc<int8_t>(B.hs.size(), st);
     check_cuda(cudaMemcpyAsync(L.buf, B.hv.get(), B.hv_n * sizeof(u64), cudaMemcpyHostToDevice, st),
                "level upload");
     check_cuda(cudaMemcpyAsync(L.sign, B.hs.data(), B.hs.size(), cudaMemcpyHostToDevice, st), "sign upload");
@@ -562,9 +576,9 @@ void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
             nx.oq[d] = total, total += up4(nx.nq[d]);
             nx.ot[d] = total, total += up4(nx.nt[d]);
         }
-        nx.buf = dev_alloc<u64>(total);
-        nx.sign = dev_alloc<int8_t>(mn);
-        uint64_t* tbuf = dev_alloc<u64>(tmp);
+        nx.buf = dev_alloc<u64>(total, st);
+        nx.sign = dev_alloc<int8_t>(mn, st);
+        uint64_t* tbuf = dev_alloc<u64>(tmp, st);
         items.clear();
         for (size_t i = 0; i < npair; ++i) {
             const size_t l = 2 * i, r = 2 * i + 1;
@@ -590,9 +604,9 @@ void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
             a.chunk0 = (uint32_t)chunk_pair.size();
             chunk_pair.insert(chunk_pair.end(), add_chunks(a.nz), (uint32_t)i);
         }
-        AddPair* d_pairs = dev_alloc<AddPair>(npair);
-        uint32_t* d_chunks = dev_alloc<uint32_t>(chunk_pair.size());
-        void* scratch = dev_alloc<uint8_t>(signed_add_scratch_bytes(npair, chunk_pair.size()));
+        AddPair* d_pairs = dev_alloc<AddPair>(npair, st);
+        uint32_t* d_chunks = dev_alloc<uint32_t>(chunk_pair.size(), st);
+        void* scratch = dev_alloc<uint8_t>(signed_add_scratch_bytes(npair, chunk_pair.size()), st);
         check_cuda(cudaMemcpyAsync(d_pairs, pairs.data(), npair * sizeof(AddPair), cudaMemcpyHostToDevice, st), "pairs");
         check_cuda(cudaMemcpyAsync(d_chunks, chunk_pair.data(), chunk_pair.size() * sizeof(uint32_t),
                                    cudaMemcpyHostToDevice, st), "chunks");
@@ -606,11 +620,11 @@ void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
             cudaMemcpyAsync(nx.sign + d, cur.sign + s, 1, cudaMemcpyDeviceToDevice, st);
         }
         check_cuda(cudaStreamSynchronize(st), "level");
-        cudaFree(d_pairs);
-        cudaFree(d_chunks);
-        cudaFree(scratch);
-        cudaFree(tbuf);
-        cur.release();
+        cudaFreeAsync(d_pairs, st);
+        cudaFreeAsync(d_chunks, st);
+        cudaFreeAsync(scratch, st);
+        cudaFreeAsync(tbuf, st);
+        cur.release(st);
         cur = std::move(nx);
         if (trace_on())
             std::fprintf(stderr, "  level of %zu nodes on the device: %zu products, Q of the first node %u limbs, %.3f s\n",
@@ -621,7 +635,8 @@ void binary_split_device(HostBlocks& blocks, Nat& Q, Nat& T, bool& tneg) {
     int8_t sg = 0;
     check_cuda(cudaMemcpy(&sg, cur.sign, 1, cudaMemcpyDeviceToHost), "sign");
     tneg = sg != 0;
-    cur.release();
+    cur.release(st);
+    check_cuda(cudaStreamSynchronize(st), "levels freed");
     cudaStreamDestroy(st);
 }
 
@@ -951,6 +966,7 @@ int main(int argc, char** argv) {
     auto device_ready = [&] {
         init_thread.join();
         if (init_rc) die("prec_gpu_init", init_rc);
+        keep_pool_memory();
         be.reset(new GpuBackend());
         set_backend(be.get());
     };

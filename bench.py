@@ -179,6 +179,24 @@ def dist_env():
     return ws, rank, local
 
 
+def ranks_max(dist, x: float, device) -> float:
+    """The largest x over the ranks of the process group (x itself without
+    one): the slowest replica's time is the job's."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_ms_per_product(slowest_total_ms: float, steps: int, world: int) -> float:
+    """Whole-job time per product: every rank timed `steps` products of its
+    own (replicas, weak scaling), so the job made steps * world products in
+    the slowest rank's time."""
+    return slowest_total_ms / steps / world
+
+
 def cpu_time(fn, max_products: int, budget_s: float):
     """Median wall time (ms) of fn() on this host thread over at most
     `max_products` calls or `budget_s` seconds (at least one call)."""
@@ -440,10 +458,7 @@ def run_ours(args):
             stage_tot[name] = stage_tot.get(name, 0.0) + ms
         flush.fill_(i & 0xFF)
     native.stream_check(sptr)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = ranks_max(dist, total_ms, dev)
     out = to.cpu().numpy().view(np.uint64)
     sha = hashlib.sha256(np.ascontiguousarray(out, dtype="<u8").tobytes()).hexdigest()
     golden = _golden_sha()
@@ -468,11 +483,7 @@ def run_ours(args):
         e2e.append(time.perf_counter() - t)
     e2e_exact = hashlib.sha256(np.ascontiguousarray(po, dtype="<u8").tobytes()).hexdigest() == golden
     plan = native.last_stats()  # the plan of the product: transform length, primes, digit width
-    e2e_ms = statistics.mean(e2e) * 1e3
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = ranks_max(dist, statistics.mean(e2e) * 1e3, dev)
     link = host_link(ho, to, stream)
 
     # ---- roofline of the dominant kernel (live events) and of the whole product
@@ -483,7 +494,7 @@ def run_ours(args):
     dom_gbs = alg[dom] / (avg[dom] * 1e-3) / 1e9
     traffic = _traffic().get(dom)
     total_alg = sum(alg.values())
-    per_product_ms = total_ms / args.steps / ws
+    per_product_ms = job_ms_per_product(total_ms, args.steps, ws)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:

@@ -77,6 +77,84 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs arg
 #undef PREC_TILE_PRODUCT
 }
 
+// The forward column pass of one prime of a 64-bit-digit product, software
+// pipelined: each CTA takes every gridDim.x-th column group of its (prime,
+// operand) and stages the next group's limbs into a second tile buffer while
+// it transforms the current one.  The single product's per-prime chains
+// launch it (five launches side by side) for the 1M x 1M class: there it
+// measured 0.1782 -> 0.1741-0.1751 ms.  As one launch over all primes the
+// one-tile kernel stays faster (71 against 77 us), and on set 3's 4M x 4M
+// it measured slower.
+constexpr int kFwdPipeTiles = 3;  // column groups per CTA
+template <int SET, int M, int C, int MR>
+__global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const ProdPtrs* __restrict__ batch) {
+    static_assert(set_wide(SET), "64-bit digits: whole limbs staged");
+    extern __shared__ uint32_t sm[];
+    constexpr int NP = sch_np(M, MR);
+    constexpr int TW = C * astride_for(M);  // words per tile buffer
+    const ProdPtrs P = select_product(args, batch);
+    const bool one = args.square || args.operand_only;
+    const int prime = args.prime0 + (one ? blockIdx.y : blockIdx.y >> 1);
+    const int operand = args.operand_only ? args.operand_only - 1 : (one ? 0 : blockIdx.y & 1);
+    const PrimeC pc = args.f.pc[prime];
+    const uint2* __restrict__ tw = args.f.tf[prime];
+    const uint32_t N2 = 1u << args.k2;
+    const int nbx = (int)(N2 / C);
+    if (args.publish && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *args.publish = P;
+    const uint64_t nl = operand ? P.lb : P.la;
+    if (nl > (1ull << (args.k - 1))) {  // the plan puts both operands in the lower half
+        if (threadIdx.x == 0) atomicOr(args.err, kDevErrPlan);
+        return;
+    }
+    const uint64_t* src = operand ? P.b : P.a;
+    uint32_t* __restrict__ dst = P.work + ((uint64_t)(prime * 2 + operand) << args.k);
+    uint32_t* cur = sm;
+    uint32_t* nxt = sm + TW;
+    int bx = blockIdx.x;
+    if (bx < nbx) stage_limbs_issue<M, C>(cur, src, N2, (uint64_t)bx * C, nl);
+    for (; bx < nbx; bx += gridDim.x) {
+        const int bn = bx + gridDim.x;
+        if (bn < nbx) {
+            stage_limbs_issue<M, C>(nxt, src, N2, (uint64_t)bn * C, nl);
+            cp_async_wait<1>();  // this tile's group done, the next one in flight
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        // the carry kernel's look-back words start at zero
+        if (blockIdx.y == 0 && args.prime0 == 0) {
+            for (int i = bx * blockDim.x + threadIdx.x; i <= P.nblk; i += nbx * blockDim.x) P.scratch[i] = 0;
+        }
+        const uint32_t c0 = (uint32_t)bx * C;
+        col_top_upper_zero<SET, M, C, MR>(cur, tw, pc);
+        __syncthreads();
+        col_passes<SET, M, 1, NP - 2, false, C, MR>(cur, tw, pc);
+        {   // bottom pass with the four-step twiddle, straight to HBM
+            using G = Geom<M, NP - 1, MR>;
+            static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
+            for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
+                const int col = w & (C - 1);
+                const uint32_t u = w / C;
+                const uint32_t* s = cur + (33 * u) * C + col;
+                const uint32_t i2 = c0 + col;
+                const uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), args.k);
+                const uint32_t g = fourstep_twiddle<SET>(args.f, prime, i2 << (M - 5), args.k);
+                uint32_t x[1][32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
+                regs_pass<SET, M, NP - 1, false, 1, MR>(x, u, tw, pc);
+                twiddle32<SET>(x[0], t, g, pc);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) dst[(uint64_t)(32 * u + q) * N2 + i2] = x[0][q];
+            }
+        }
+        __syncthreads();  // every thread is done with `cur` before it is refilled
+        uint32_t* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+}
+
 // One tile of the forward column pass at the indices ix (a persistent kernel's).
 template <int SET, int M, int C, int MR>
 __device__ __forceinline__ void fwd_cols_tile(const ProdArgs& args, const ProdPtrs* __restrict__ batch,

@@ -277,6 +277,24 @@ __device__ __forceinline__ void stage_limbs(uint32_t* sm, const uint64_t* __rest
     cp_async_wait<0>();
 }
 
+// stage_limbs without the wait: the copies of one tile as one committed
+// group, left in flight (the pipelined forward columns prefetch the next tile)
+template <int M, int C>
+__device__ __forceinline__ void stage_limbs_issue(uint32_t* sm, const uint64_t* __restrict__ g, uint64_t ld,
+                                                  uint64_t c0, uint64_t valid) {
+    constexpr int H = 1 << (M - 1);
+    const uint32_t* __restrict__ g32 = reinterpret_cast<const uint32_t*>(g);
+    for (int w = threadIdx.x; w < H * C; w += blockDim.x) {
+        const int r = w / C, col = w % C;
+        const uint64_t idx = (uint64_t)r * ld + c0 + col;
+        const bool in = idx < valid;
+        const uint32_t* src = in ? g32 + 2 * idx : g32;  // 0 bytes read (zero fill) past the operand
+        cp_async4(sm + padded(r) * C + col, src, in ? 4 : 0);
+        cp_async4(sm + padded(r + H) * C + col, in ? src + 1 : g32, in ? 4 : 0);
+    }
+    cp_async_commit();
+}
+
 template <int M, int C>
 __device__ __forceinline__ void stage_cols(uint32_t* sm, const uint32_t* __restrict__ g, uint64_t ld, uint64_t c0,
                                            uint64_t valid) {

@@ -19,9 +19,16 @@
 // moves whole 32-byte sectors.
 // Template parameters: SET prime set, M = log2 N1 (column length), C
 // columns per CTA (launched with 32*C threads), MR the pass radix cap (MR = 6: a 2^11-point column runs
-// as a radix-64 and a radix-32 pass; MR = 4: radix-8, -8, -32).  The
-// instantiated (SET, M, C, MR) configurations are PREC_COLS_CONFIGS; the
-// autotuner picks C and MR per transform length.
+// as a radix-64 and a radix-32 pass; MR = 4: radix-8, -8, -32), K2 =
+// log2 N2 (the row length, the stride between a column's elements) as a
+// constant, or 0: from the arguments.  The instantiated (SET, M, C, MR)
+// configurations are PREC_COLS_CONFIGS, with K2 = 0; the autotuner picks C
+// and MR per transform length.  The default configuration of every
+// transform length also has a K2 instantiation (PREC_COLS_*_K2_CONFIGS,
+// ntt_cols_fwd_k2.cu, ntt_cols_inv_k2.cu).  Its global addresses are a
+// constant offset from one base per item.  At 2^21 points on the 64-bit plan
+// the forward columns measured 71.5 -> 63.1 us, and the inverse columns
+// 34.8 -> 32.8 us.
 #pragma once
 #include "ntt_engine.cuh"
 
@@ -63,14 +70,16 @@ __device__ __forceinline__ void col_top_upper_zero(uint32_t* sm, const uint2* __
 // The forward column pass: column group x (C columns) and y = prime*2 +
 // operand (or just the prime for a square or a launch of one operand) of
 // product z; nx = column groups per (prime, operand).
-template <int SET, int M, int C, int MR>
+template <int SET, int M, int C, int MR, int K2 = 0>
 __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
+#define PREC_K2 K2
 #define PREC_TILE_X blockIdx.x
 #define PREC_TILE_Y blockIdx.y
 #define PREC_TILE_NX gridDim.x
 #define PREC_TILE_PRODUCT select_product(args, batch)
 #include "ntt_cols_fwd_body.inc"
+#undef PREC_K2
 #undef PREC_TILE_X
 #undef PREC_TILE_Y
 #undef PREC_TILE_NX
@@ -86,9 +95,10 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs arg
 // one-tile kernel stays faster (71 against 77 us), and on set 3's 4M x 4M
 // it measured slower.
 constexpr int kFwdPipeTiles = 3;  // column groups per CTA
-template <int SET, int M, int C, int MR>
+template <int SET, int M, int C, int MR, int K2>
 __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     static_assert(set_wide(SET), "64-bit digits: whole limbs staged");
+    static_assert(K2 > 0, "a constant row length");
     extern __shared__ uint32_t sm[];
     constexpr int NP = sch_np(M, MR);
     constexpr int TW = C * astride_for(M);  // words per tile buffer
@@ -98,16 +108,17 @@ __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const P
     const int operand = args.operand_only ? args.operand_only - 1 : (one ? 0 : blockIdx.y & 1);
     const PrimeC pc = args.f.pc[prime];
     const uint2* __restrict__ tw = args.f.tf[prime];
-    const uint32_t N2 = 1u << args.k2;
-    const int nbx = (int)(N2 / C);
+    constexpr uint32_t N2 = 1u << K2;
+    constexpr int KK = M + K2;  // log2 of the transform length
+    constexpr int nbx = (int)(N2 / C);
     if (args.publish && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *args.publish = P;
     const uint64_t nl = operand ? P.lb : P.la;
-    if (nl > (1ull << (args.k - 1))) {  // the plan puts both operands in the lower half
+    if (nl > (1ull << (KK - 1))) {  // the plan puts both operands in the lower half
         if (threadIdx.x == 0) atomicOr(args.err, kDevErrPlan);
         return;
     }
     const uint64_t* src = operand ? P.b : P.a;
-    uint32_t* __restrict__ dst = P.work + ((uint64_t)(prime * 2 + operand) << args.k);
+    uint32_t* __restrict__ dst = P.work + ((uint64_t)(prime * 2 + operand) << KK);
     uint32_t* cur = sm;
     uint32_t* nxt = sm + TW;
     int bx = blockIdx.x;
@@ -137,8 +148,8 @@ __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const P
                 const uint32_t u = w / C;
                 const uint32_t* s = cur + (33 * u) * C + col;
                 const uint32_t i2 = c0 + col;
-                const uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), args.k);
-                const uint32_t g = fourstep_twiddle<SET>(args.f, prime, i2 << (M - 5), args.k);
+                const uint32_t t = fourstep_twiddle<SET>(args.f, prime, i2 * brev_bits(u, M - 5), KK);
+                const uint32_t g = fourstep_twiddle<SET>(args.f, prime, i2 << (M - 5), KK);
                 uint32_t x[1][32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
@@ -159,11 +170,13 @@ __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const P
 template <int SET, int M, int C, int MR>
 __device__ __forceinline__ void fwd_cols_tile(const ProdArgs& args, const ProdPtrs* __restrict__ batch,
                                               const TileIdx& ix, uint32_t* sm) {
+#define PREC_K2 0
 #define PREC_TILE_X ix.bx
 #define PREC_TILE_Y ix.by
 #define PREC_TILE_NX ix.nbx
 #define PREC_TILE_PRODUCT select_product_at(args, batch, ix.bz)
 #include "ntt_cols_fwd_body.inc"
+#undef PREC_K2
 #undef PREC_TILE_X
 #undef PREC_TILE_Y
 #undef PREC_TILE_NX
@@ -172,13 +185,15 @@ __device__ __forceinline__ void fwd_cols_tile(const ProdArgs& args, const ProdPt
 
 // The inverse column pass: column group x, prime args.prime0 + y of
 // product z.
-template <int SET, int M, int C, int MR>
+template <int SET, int M, int C, int MR, int K2 = 0>
 __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_inv_cols(ProdArgs args, const ProdPtrs* __restrict__ batch) {
     extern __shared__ uint32_t sm[];
+#define PREC_K2 K2
 #define PREC_TILE_X blockIdx.x
 #define PREC_TILE_Y blockIdx.y
 #define PREC_TILE_PRODUCT select_product(args, batch)
 #include "ntt_cols_inv_body.inc"
+#undef PREC_K2
 #undef PREC_TILE_X
 #undef PREC_TILE_Y
 #undef PREC_TILE_PRODUCT
@@ -188,10 +203,12 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_inv_cols(ProdArgs arg
 template <int SET, int M, int C, int MR>
 __device__ __forceinline__ void inv_cols_tile(const ProdArgs& args, const ProdPtrs* __restrict__ batch,
                                               const TileIdx& ix, uint32_t* sm) {
+#define PREC_K2 0
 #define PREC_TILE_X ix.bx
 #define PREC_TILE_Y ix.by
 #define PREC_TILE_PRODUCT select_product_at(args, batch, ix.bz)
 #include "ntt_cols_inv_body.inc"
+#undef PREC_K2
 #undef PREC_TILE_X
 #undef PREC_TILE_Y
 #undef PREC_TILE_PRODUCT
@@ -214,6 +231,30 @@ __device__ __forceinline__ void inv_cols_tile(const ProdArgs& args, const ProdPt
     X(2, 11, 8, 4) X(2, 11, 4, 6) X(2, 11, 8, 6) X(3, 10, 4, 6) X(3, 10, 8, 6) X(3, 11, 4, 4)             \
     X(3, 11, 8, 4) X(3, 11, 4, 6) X(3, 11, 8, 6) X(3, 12, 4, 6)
 
+// (SET, M, C, MR, K2) of the default configurations (sets 0 and 2: N1 =
+// 2^floor(k/2); sets 1 and 3: N2 = 2^13), compiled with a constant row
+// length.  The inverse columns of sets 2 and 3 are set 0's and set 1's.
+#define PREC_COLS_FWD_K2_CONFIGS(X)                                                                        \
+    X(0, 6, 8, 6, 7) X(0, 7, 8, 6, 7) X(0, 7, 8, 6, 8) X(0, 8, 8, 6, 8) X(0, 8, 8, 6, 9) X(0, 9, 8, 6, 9)   \
+    X(0, 9, 8, 6, 10) X(0, 10, 8, 6, 10) X(0, 10, 8, 6, 11) X(0, 11, 8, 6, 11) X(0, 11, 8, 6, 12)           \
+    X(2, 9, 8, 6, 9) X(2, 9, 8, 6, 10) X(2, 10, 8, 6, 10) X(2, 10, 8, 6, 11) X(2, 11, 8, 6, 11)             \
+    X(1, 11, 8, 6, 13) X(1, 12, 4, 6, 13) X(1, 13, 4, 6, 13) X(3, 10, 8, 6, 13) X(3, 11, 8, 6, 13)         \
+    X(3, 12, 4, 6, 13)
+#define PREC_COLS_INV_K2_CONFIGS(X)                                                                        \
+    X(0, 6, 8, 6, 7) X(0, 7, 8, 6, 7) X(0, 7, 8, 6, 8) X(0, 8, 8, 6, 8) X(0, 8, 8, 6, 9) X(0, 9, 8, 6, 9)   \
+    X(0, 9, 8, 6, 10) X(0, 10, 8, 6, 10) X(0, 10, 8, 6, 11) X(0, 11, 8, 6, 11) X(0, 11, 8, 6, 12)           \
+    X(1, 10, 8, 6, 13) X(1, 11, 8, 6, 13) X(1, 12, 4, 6, 13) X(1, 13, 4, 6, 13)
+
 inline size_t col_smem(int m, int cg) { return (size_t)cg * astride_for(m) * sizeof(uint32_t); }
+
+// the K2 instantiations (ntt_cols_fwd_k2.cu, ntt_cols_inv_k2.cu): launch the
+// one matching (set, a.k1, cg, mr, a.k2) and return true, or return false.
+// one_prime: a single product's launch for one prime (the per-prime chains)
+bool launch_fwd_cols_k2(int set, const ProdArgs& a, int cg, int mr, dim3 grid, size_t smem, cudaStream_t st,
+                        const ProdPtrs* batch, bool one_prime);
+bool launch_inv_cols_k2(int set, const ProdArgs& a, int cg, int mr, dim3 grid, size_t smem, cudaStream_t st,
+                        const ProdPtrs* batch);
+int configure_fwd_cols_k2();
+int configure_inv_cols_k2();
 
 }  // namespace precgpu

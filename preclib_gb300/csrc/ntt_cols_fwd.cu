@@ -10,14 +10,7 @@ void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
     col_config(set_base(set), a.k1, a.cg, a.cmr, cg, mr);
     const dim3 grid((1u << a.k2) / cg, (a.square || a.operand_only ? 1 : 2) * nprimes, count);
     const size_t smem = col_smem(a.k1, cg);
-    // one prime of a single product's per-prime chains on the first
-    // five-prime set at 2^10-point columns (the 1M x 1M class), both operands
-    // at once: the pipelined kernel.  (On set 3's 4M x 4M it measured slower,
-    // 0.723 -> 0.735 ms; for the host-pointer form's launches of one uploaded
-    // operand each, e2e 0.344 -> 0.353 ms.)
-    if (nprimes == 1 && !batch && !a.operand_only && a.k1 == 10 && cg == 8 && mr == 6 && set == kWideSet) {
-        const dim3 pg((grid.x + kFwdPipeTiles - 1) / kFwdPipeTiles, grid.y, grid.z);
-        launch_kernel(k_fwd_cols_pipe<kWideSet, 10, 8, 6>, pg, 256, 2 * smem, st, a, batch);
+    if (launch_fwd_cols_k2(set, a, cg, mr, grid, smem, st, batch, nprimes == 1)) {
         count_launches(1);
         return;
     }
@@ -33,9 +26,7 @@ void launch_fwd_cols(int set, const ProdArgs& a, cudaStream_t st, const ProdPtrs
 }
 
 int configure_fwd_cols() {
-    cudaError_t e = cudaSuccess;
-    e = cudaFuncSetAttribute(k_fwd_cols_pipe<kWideSet, 10, 8, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(2 * col_smem(10, 8)));
+    cudaError_t e = (cudaError_t)configure_fwd_cols_k2();
 #define X(S, MM, CC, RR)                                                                                   \
     if (!e) e = cudaFuncSetAttribute(k_fwd_cols<S, MM, CC, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)col_smem(MM, CC));

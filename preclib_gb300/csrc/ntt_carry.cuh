@@ -270,47 +270,69 @@ __device__ __forceinline__ void crt_carry_tile(const ProdArgs& args, const ProdP
     const int nb = bhi - blo;
     const int per = (nb + blockDim.x - 1) / blockDim.x;  // aggregates per thread
     const int b0 = blo + threadIdx.x * per, b1 = min(b0 + per, bhi);
-    // this thread's run of blocks as one carry element.  The aggregates are
-    // loaded kAggBatch at a time in one unrolled group (independent loads in
-    // flight together, not one L2 round trip each); a run of at most
-    // kAggBatch blocks -- every product up to 2^21 limbs -- stays in
-    // registers for the second pass.  Past the run: G = 0, P = 1.
-    constexpr int kAggBatch = 8;
-    uint32_t held[kAggBatch];
-    bool tG = false, tP = true;
-    for (int base = b0; base < b1; base += kAggBatch) {
-#pragma unroll
-        for (int i = 0; i < kAggBatch; ++i) held[i] = base + i < b1 ? __ldcg(&agg[base + i]) : 2u;
-#pragma unroll
-        for (int i = 0; i < kAggBatch; ++i) {
-            tG = (held[i] & 1u) || (tG && (held[i] & 2u));
-            tP = tP && (held[i] & 2u);
-        }
-    }
+    const int n = b1 > b0 ? b1 - b0 : 0;  // this thread's run of blocks
     auto chunk_in = [&](bool, bool) -> bool { return cin_chunk; };
-    bool c = block_carry(tG, tP, sh, chunk_in);  // carry into this thread's first block
-    auto enter = [&](int b, uint32_t a) {
-        if (c) {
-            // the carry enters block b: +1 ripples through its all-ones limbs
-            const uint64_t lim_end = min((uint64_t)(b + 1) * BL, PP.lout);
-            for (uint64_t m = (uint64_t)b * BL; m < lim_end; ++m) {
-                const uint64_t x = __ldcg(&PP.out[m]) + 1;
-                PP.out[m] = x;
-                if (x != 0) break;
+    // the carry enters block b: +1 ripples through its all-ones limbs
+    auto ripple = [&](int b) {
+        const uint64_t lim_end = min((uint64_t)(b + 1) * BL, PP.lout);
+        for (uint64_t m = (uint64_t)b * BL; m < lim_end; ++m) {
+            const uint64_t x = __ldcg(&PP.out[m]) + 1;
+            PP.out[m] = x;
+            if (x != 0) break;
+        }
+    };
+    // The aggregates are loaded kAggBatch at a time in one unrolled group
+    // (independent loads in flight together, not one L2 round trip each).
+    constexpr int kAggBatch = 16;
+    bool cout;  // the carry out of this thread's last block
+    if (per <= 64) {
+        // the run as bit masks (bit i: block b0 + i; G and P, with G = 0,
+        // P = 1 past the run): the run's own aggregate and, once the carry
+        // into it is known, the carry into each of its blocks come from one
+        // carry-chain addition each (a product up to 2^24 limbs)
+        uint64_t gm = 0, pm = 0;
+        for (int base = 0; base < per; base += kAggBatch) {
+            uint32_t h[kAggBatch];
+#pragma unroll
+            for (int i = 0; i < kAggBatch; ++i) h[i] = base + i < n ? __ldcg(&agg[b0 + base + i]) : 2u;
+#pragma unroll
+            for (int i = 0; i < kAggBatch; ++i) {
+                gm |= (uint64_t)(h[i] & 1u) << (base + i);
+                pm |= (uint64_t)((h[i] >> 1) & 1u) << (base + i);
             }
         }
-        c = (a & 1u) || (c && (a & 2u));
-    };
-    if (per <= kAggBatch) {
-#pragma unroll
-        for (int i = 0; i < kAggBatch; ++i)
-            if (b0 + i < b1) enter(b0 + i, held[i]);
+        const u128 A = (u128)(gm | pm), B = (u128)gm;
+        const uint64_t nmask = n >= 64 ? ~0ull : ((1ull << n) - 1);
+        const bool tG = (uint64_t)(((A + B) ^ A ^ B) >> n) & 1;  // carry out of the run, carry-in 0
+        const bool tP = (pm & nmask) == nmask;
+        const bool c = block_carry(tG, tP, sh, chunk_in);  // carry into this thread's first block
+        const u128 cc = (A + B + (c ? 1u : 0u)) ^ A ^ B;   // bit i: carry into block b0 + i
+        for (uint64_t enter = (uint64_t)cc & nmask; enter; enter &= enter - 1) ripple(b0 + __ffsll((long long)enter) - 1);
+        cout = (uint64_t)(cc >> n) & 1;
     } else {
-        for (int b = b0; b < b1; ++b) enter(b, __ldcg(&agg[b]));
+        // longer runs: two passes over the aggregates
+        bool tG = false, tP = true;
+        for (int base = b0; base < b1; base += kAggBatch) {
+            uint32_t h[kAggBatch];
+#pragma unroll
+            for (int i = 0; i < kAggBatch; ++i) h[i] = base + i < b1 ? __ldcg(&agg[base + i]) : 2u;
+#pragma unroll
+            for (int i = 0; i < kAggBatch; ++i) {
+                tG = (h[i] & 1u) || (tG && (h[i] & 2u));
+                tP = tP && (h[i] & 2u);
+            }
+        }
+        bool c = block_carry(tG, tP, sh, chunk_in);  // carry into this thread's first block
+        for (int b = b0; b < b1; ++b) {
+            const uint32_t a = __ldcg(&agg[b]);
+            if (c) ripple(b);
+            c = (a & 1u) || (c && (a & 2u));
+        }
+        cout = c;
     }
     if (b0 < bhi && b1 == bhi) {  // the thread holding the last block
-        if (chunked && !args.crt_last) args.chunk_words[2 * args.crt_chunk + 3] = c ? 1u : 0u;
-        else if (c) atomicOr(args.err, kDevErrCarry);  // a product fits La+Lb limbs
+        if (chunked && !args.crt_last) args.chunk_words[2 * args.crt_chunk + 3] = cout ? 1u : 0u;
+        else if (cout) atomicOr(args.err, kDevErrCarry);  // a product fits La+Lb limbs
     }
 }
 

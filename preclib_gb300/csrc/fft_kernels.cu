@@ -332,14 +332,16 @@ constexpr int kFftCarryBlockLimbs = kFftCarryThreads * kFftCarryLimbs;
 // (maps composed by warp shuffles and a block scan), limbs written -- below
 // La+Lb to the output, above it to scratch -- and the block's composed map
 // published.  Phase 2 (the last block to finish, fence + atomic counter):
-// composes the block maps in order, adds each nonzero block carry-in into
-// its block (+1 ripples through all-ones limbs, -1 through zero limbs; rare),
-// and checks that every limb past La+Lb and the final carry are zero.
+// loads the block maps into shared memory (one load per thread, all in
+// flight at once), composes them in order, adds each nonzero block carry-in
+// into its block (+1 ripples through all-ones limbs, -1 through zero limbs;
+// rare), and checks that every limb past La+Lb and the final carry are zero.
 // scratch (the transform buffer, free by now): [0] counter, [1 .. nblk]
 // block maps, then the limbs from La+Lb up.
 __global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(const FftArgs* __restrict__ fa) {
     const FftArgs f = *fa;
     __shared__ uint32_t s_wmap[kFftCarryThreads / 32];
+    __shared__ uint32_t s_bmap[kFftCarryThreads];
     __shared__ uint32_t s_last;
     const double dist = *f.maxdist;
     if (!(dist <= 0.25)) {  // also NaN / inf: nothing is written
@@ -425,6 +427,11 @@ __global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(const FftArgs* _
     __syncthreads();
     if (!s_last) return;
     __threadfence();
+    // (one L2 round trip per block map, in the serial loop below, made this
+    // kernel 14 us long at 3000 x 3000 limbs)
+    const bool staged = nblk <= kFftCarryThreads;
+    if (staged && (int)threadIdx.x < nblk) s_bmap[threadIdx.x] = (uint32_t)__ldcg(&bmap[threadIdx.x]);
+    __syncthreads();
     if (threadIdx.x == 0) {
         int c = 0;
         for (int bk = 0; bk < nblk; ++bk) {
@@ -437,7 +444,7 @@ __global__ void __launch_bounds__(kFftCarryThreads) k_fft_carry(const FftArgs* _
                     if (c > 0 ? old != ~0ull : old != 0) break;
                 }
             }
-            c = map_apply((uint32_t)__ldcg(&bmap[bk]), c);
+            c = map_apply(staged ? s_bmap[bk] : (uint32_t)__ldcg(&bmap[bk]), c);
         }
         if (c != 0) atomicOr(f.err, kDevErrCarry);
     }

@@ -66,6 +66,26 @@ def test_both_paths_each_length(gpu, wide):
         gpu.set_wide_digits(prev)
 
 
+@pytest.mark.parametrize("wide,k", [(False, 20), (False, 21), (False, 23), (True, 19), (True, 20), (True, 22)])
+def test_large_lengths_vs_oracle(gpu, wide, k):
+    """The transform lengths above 2^19 that no golden digest covers, against the
+    oracle: the default configurations of sets 0 and 2, whose column kernels
+    run compiled for their row length."""
+    n = 1 << (k - 1 if wide else k - 2)  # balanced operands filling a 2^k-point transform
+    a = O.splitmix64(k * 7 + 1, n)
+    b = O.splitmix64(k * 7 + 2, n)
+    a[-1] |= np.uint64(1 << 63)
+    b[-1] |= np.uint64(1 << 63)
+    prev = gpu.set_wide_digits(wide)
+    try:
+        got = gpu.mul(a, b, ntt=True)
+        st = gpu.last_stats()
+    finally:
+        gpu.set_wide_digits(prev)
+    assert st.log2_n == k and st.path == 1 and st.digit_bits == (64 if wide else 32)
+    assert np.array_equal(got, O.mul_ntt(a, b))
+
+
 def test_zero_and_padding(gpu):
     z = np.zeros(5, np.uint64)
     a = O.splitmix64(3, 9000)

@@ -91,9 +91,10 @@ __global__ void __launch_bounds__(256, cols_minb(M, MR)) k_fwd_cols(ProdArgs arg
 // operand) and stages the next group's limbs into a second tile buffer while
 // it transforms the current one.  The single product's per-prime chains
 // launch it (five launches side by side) for the 1M x 1M class: there it
-// measured 0.1782 -> 0.1741-0.1751 ms.  As one launch over all primes the
-// one-tile kernel stays faster (71 against 77 us), and on set 3's 4M x 4M
-// it measured slower.
+// measured 0.1782 -> 0.1741-0.1751 ms, and with both kernels compiled for
+// the constant row length 0.1690 -> 0.1672 ms (2 or 4 tiles per CTA: 0.1679,
+// 0.1685-0.1692).  As one launch over all primes the one-tile kernel stays
+// faster (71 against 77 us), and on set 3's 4M x 4M it measured slower.
 constexpr int kFwdPipeTiles = 3;  // column groups per CTA
 template <int SET, int M, int C, int MR, int K2>
 __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const ProdPtrs* __restrict__ batch) {

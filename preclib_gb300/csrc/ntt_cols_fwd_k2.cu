@@ -10,9 +10,10 @@ bool launch_fwd_cols_k2(int set, const ProdArgs& a, int cg, int mr, dim3 grid, s
                         const ProdPtrs* batch, bool one_prime) {
     // one prime of a single product's per-prime chains on the first
     // five-prime set at 2^10 x 2^11 points (the 1M x 1M class), both
-    // operands at once: the pipelined kernel.  (On set 3's 4M x 4M it
-    // measured slower, 0.723 -> 0.735 ms; for the host-pointer form's
-    // launches of one uploaded operand each, e2e 0.344 -> 0.353 ms.)
+    // operands at once: the pipelined kernel (1M x 1M 0.1690 -> 0.1672 ms
+    // against the one-tile kernel).  On set 3's 4M x 4M it measured slower
+    // (0.688 -> 0.705 ms), and so did the host-pointer form's launches of
+    // one uploaded operand each (e2e 0.344 -> 0.353 ms).
     if (one_prime && !batch && !a.operand_only && set == kWideSet && a.k1 == 10 && a.k2 == 11 && cg == 8 &&
         mr == 6) {
         const dim3 pg((grid.x + kFwdPipeTiles - 1) / kFwdPipeTiles, grid.y, grid.z);

@@ -144,6 +144,7 @@ __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const P
         {   // bottom pass with the four-step twiddle, straight to HBM
             using G = Geom<M, NP - 1, MR>;
             static_assert(G::LO == 0 && G::RB == 5, "bottom pass covers bits 0..4");
+            const double ip = 4294967296.0 / (double)pc.p;  // 2^32 / p for twiddle32_shoup
             for (int w = threadIdx.x; w < (C << G::LGI); w += blockDim.x) {
                 const int col = w & (C - 1);
                 const uint32_t u = w / C;
@@ -155,7 +156,7 @@ __global__ void __launch_bounds__(256, 3) k_fwd_cols_pipe(ProdArgs args, const P
 #pragma unroll
                 for (int q = 0; q < 32; ++q) x[0][q] = s[q * C];
                 regs_pass<SET, M, NP - 1, false, 1, MR>(x, u, tw, pc);
-                twiddle32<SET>(x[0], t, g, pc);
+                twiddle32_shoup<SET>(x[0], t, g, pc, ip);
 #pragma unroll
                 for (int q = 0; q < 32; ++q) dst[(uint64_t)(32 * u + q) * N2 + i2] = x[0][q];
             }
